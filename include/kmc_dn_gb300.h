@@ -1,0 +1,230 @@
+/*
+ * kmc_dn_gb300.h -- C ABI of the GB300 (sm_103a) kinetic Monte Carlo engine
+ * for dopant networks.
+ *
+ * This is the drop-in boundary for the hop loop of MUTUEL/kmc_dn.  The
+ * reference reaches its native loop through ctypes on a Go c-shared library
+ * (goSimulation/pythonBind.py:49-92, goSimulation/parrallelSimulationBind.py:
+ * 50-66) whose exports take GoSlice {data, len, cap} views of FP64 host
+ * arrays (goSimulation/simulationWrapper.go:83-315).  The entry points below
+ * take plain pointers and sizes, return a status code, and never abort the
+ * host process.  Each declaration names the reference interface it replaces.
+ *
+ * Conventions
+ *   - S = N + P sites, acceptors first, then electrodes (the reference's
+ *     site order, kmc_dopant_networks.py:657-695).  Pair tables are S*S,
+ *     row-major (from, to).
+ *   - "device" pointers are CUDA device (or managed) memory; "host"
+ *     pointers are ordinary host memory.
+ *   - stream: a cudaStream_t passed as void* (NULL = the legacy default
+ *     stream).  Device-pointer entry points are asynchronous on that stream;
+ *     host-pointer entry points synchronise before returning.
+ *   - Return value: KMC_OK (0) or a negative KMC_ERR_* code; the message of
+ *     the last error on the calling thread is read with kmc_last_error().
+ *     Per-chain problems (no allowed transition, non-finite total rate)
+ *     are reported per chain in a status array and do not fail the call.
+ */
+#ifndef KMC_DN_GB300_H
+#define KMC_DN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KMC_OK 0
+#define KMC_ERR_INVALID (-1)    /* bad sizes, pointers or options            */
+#define KMC_ERR_CUDA (-2)       /* a CUDA runtime call failed                */
+#define KMC_ERR_OOM (-3)        /* device or host allocation failed          */
+#define KMC_ERR_TIMEOUT (-4)    /* hop or wall-clock budget exhausted        */
+#define KMC_ERR_NONFINITE (-5)  /* total rate zero, negative or non-finite   */
+#define KMC_ERR_CANCELLED (-6)  /* stopped through the cancel word           */
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+int kmc_version(void);
+
+/* Copy the last error message of the calling thread into buf (always NUL
+ * terminated); returns the last status code.  No reference counterpart: the
+ * Go library has no error channel (goSimulation/pythonBind.py:81). */
+int kmc_last_error(char *buf, size_t len);
+
+/* ------------------------------------------------------------------------ */
+/* Plain single-chain FP64 hop loop                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Workspace bytes kmc_simulate_f64 needs for S sites. */
+size_t kmc_simulate_f64_workspace_size(int32_t n_sites);
+
+/*
+ * One chain, FP64 throughout, with the semantics of the reference's numba
+ * loop _simulate_discrete_record (kmc_dopant_networks.py:33-135), which
+ * kmc_dn.python_simulation / makeSimulation call (:513-619):
+ *   - starts from `occupation` and leaves the final state in it;
+ *   - electrode_occupation is accumulated (+1 = a hole into the electrode);
+ *   - each hop draws two uniforms, clock first: dt = -log(1-u1) / total,
+ *     then the first row-major pair k with cum_k/total >= u2 (:100-110);
+ *   - record != 0: traffic[from*S+to] += 1 and occupations_in_time[i] +=
+ *     dt for every acceptor occupied AFTER the hop (:126-130).
+ * uniforms: NULL, or 2*hops replay values in (0,1) (device).  When NULL the
+ * uniforms come from Philox4x32-10 keyed by seed.
+ * All arrays are device pointers; hop_log (2*hops int32) may be NULL;
+ * time_out and status_out are single device values.  workspace must hold
+ * kmc_simulate_f64_workspace_size(S) bytes.
+ */
+int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, double kT,
+                     double I_0, double R, uint8_t *occupation, const double *distances,
+                     const double *E_constant, const double *site_energies,
+                     const double *transitions_constant, int64_t *electrode_occupation,
+                     int64_t hops, int32_t record, double *traffic,
+                     double *occupations_in_time, const double *uniforms, uint64_t seed,
+                     int32_t *hop_log, double *time_out, int32_t *status_out,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Batched FP32 engine                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* Record conventions. */
+#define KMC_RECORD_NONE 0
+#define KMC_RECORD_NUMBA 1   /* traffic[f,t] += 1; occupancy credited after the hop
+                                (kmc_dopant_networks.py:126-130) */
+#define KMC_RECORD_GO 2      /* traffic[f,t] += 1, traffic[t,f] -= 1; occupancy
+                                credited before the hop (simulation.go:309-317) */
+
+/*
+ * Launch description of the batched engine.  Every pointer is device
+ * memory.  A "table" is one geometry instance: S*S interleaved float pairs
+ * (L, B) with L = log2(nu * transitions_constant[i][j]) and B = I_0*R /
+ * distances[i][j] for acceptor pairs, 0 otherwise (built from the FP64
+ * tables by kmc_build_tables).  Chains name a table; many chains may share
+ * one.  Per-site pools (N entries per chain), per-electrode pools (P
+ * entries per chain) and per-pair pools (S*S entries per chain) are indexed
+ * by the chain's offsets.
+ *
+ * The work list assigns chains to warps: item w is 32/G chain ids
+ * work[w*(32/G) + s] (-1 = empty slot) run by one warp, G lanes per chain.
+ * Chains in one item should have similar size and hop budget.
+ *
+ * Each launch advances every listed chain by min(hops_total - hops_done,
+ * max_hops_per_launch) hops (max_hops_per_launch a multiple of reanchor),
+ * accumulating time, electrode_occupation and the record pools, and
+ * writing back occupation and hops_done, so a run can be split into
+ * launches (serving, checkpoint/resume) with results independent of the
+ * split.
+ */
+typedef struct kmc_batch {
+    /* tables */
+    int32_t n_tables;
+    int32_t max_sites;              /* >= S of every chain in the launch       */
+    const int32_t *tab_N;           /* [n_tables] acceptors                    */
+    const int32_t *tab_P;           /* [n_tables] electrodes (<= 64)           */
+    const int64_t *tab_off;         /* [n_tables] offset in floats into tab_LB */
+    const float *tab_LB;            /* pair tables, 2*S*S floats each          */
+    /* chains */
+    int32_t n_chains;
+    int32_t lanes_per_chain;        /* G in {4, 8, 16, 32}                     */
+    const int32_t *chain_tab;       /* [n_chains]                              */
+    const float *chain_kT;          /* [n_chains]                              */
+    const int64_t *chain_site_off;  /* [n_chains] offset into per-site pools   */
+    const int64_t *chain_el_off;    /* [n_chains] offset into electrode pools  */
+    const int64_t *chain_pair_off;  /* [n_chains] offset into traffic pool     */
+    const float *E_constant;        /* site pool: constant site energies       */
+    const float *el_energy;         /* electrode pool: electrode energies      */
+    uint8_t *occupation;            /* site pool, in/out                       */
+    int64_t *electrode_occupation;  /* electrode pool, accumulated             */
+    double *time;                   /* [n_chains] accumulated                  */
+    int64_t *hops_done;             /* [n_chains] in/out                       */
+    const int64_t *hops_total;      /* [n_chains]                              */
+    const uint64_t *stream;         /* [n_chains] RNG stream ids               */
+    int32_t *status;                /* [n_chains] out: KMC_OK or KMC_ERR_*     */
+    unsigned long long *n_pairs;    /* [n_chains] accumulated allowed pairs    */
+    double *occ_time;               /* site pool: time-weighted occupancy      */
+    double *occ_since;              /* site pool: scratch for occ_time         */
+    int32_t *traffic;               /* pair pool                               */
+    /* work list */
+    const int32_t *work;
+    int32_t n_work;
+    int32_t record;                 /* KMC_RECORD_*                            */
+    int32_t reanchor;               /* hops between FP32 energy re-anchors     */
+    int32_t warps_per_block;        /* 1..8                                    */
+    int64_t max_hops_per_launch;
+    uint64_t seed;
+    const double *replay;           /* optional 2 uniforms per hop per chain   */
+    const int64_t *replay_off;      /* [n_chains] offset into replay           */
+    const volatile int32_t *cancel; /* optional host-mapped cancel word        */
+} kmc_batch;
+
+/*
+ * Build one FP32 pair table (2*S*S floats at tab_LB) from FP64 device
+ * tables: L = log2(nu*tc), B = I_0*R/d for acceptor pairs.  Restates the
+ * constant part of the rate (calc_transitions_constant,
+ * kmc_dopant_networks.py:824-830) and the Coulomb term of dE
+ * (:72-75, simulation.go:67-68) in the form the engine consumes.
+ */
+int kmc_build_table(int32_t n_acceptors, int32_t n_electrodes, double nu, double I_0, double R,
+                    const double *distances, const double *transitions_constant,
+                    float *tab_LB, void *stream);
+
+/*
+ * Constant site energies of many chains on one geometry from the Laplace
+ * basis fields sampled at the acceptors (the linear superposition that
+ * replaces a FEniCS solve per voltage vector, kmc_dopant_networks.py:
+ * 798-821 + 865-899):
+ *   E_constant[c][i] = sum_e V[c][e]*basis[e][i] + mu*basis[n_el][i] + comp[i]
+ *   el_energy[c][e]  = V[c][e]
+ * basis: (n_el+1) x N FP64, V: n_chains x n_el FP64, comp: N FP64.
+ * Outputs: E_constant FP32 (n_chains x N, row stride N), el_energy FP32.
+ */
+int kmc_site_energies(int32_t n_chains, int32_t n_acceptors, int32_t n_electrodes,
+                      const double *basis, const double *voltages, double mu,
+                      const double *comp, float *E_constant, float *el_energy, void *stream);
+
+/*
+ * Run one launch of the batched engine (device pointers, asynchronous).
+ * Replaces the goroutine-per-chain parallelSimulations
+ * (goSimulation/simulationWrapper.go:275-315) and the per-chain Go
+ * simulate loop (simulation.go:194-325).
+ */
+int kmc_run_batch(const kmc_batch *batch, void *stream);
+
+/* Lanes-per-chain choices compiled into the engine: bit k set = G of 2^k. */
+int kmc_engine_lane_options(void);
+
+/* Measure the device's ex2 (SFU) throughput in ex2 results per second: the
+ * roofline of the rate evaluation.  Synchronous, on the current device.  No
+ * reference counterpart (measurement support). */
+int kmc_measure_ex2_rate(double *ex2_per_second);
+
+/*
+ * Host-buffer batch run: chains on shared geometries, FP64 host inputs,
+ * copies in and out inside the call (synchronous).  This is the
+ * reference-facing batched call with host buffers, the counterpart of
+ * parallelSimulations (goSimulation/simulationWrapper.go:275-315) fed by
+ * parrallelSimulation.runSimulation (goSimulation/parrallelSimulationBind.py:
+ * 50-66), with per-geometry instead of per-chain tables.
+ *   geometries g: N[g], P[g], nu[g], I_0[g], R[g], distances/tc at
+ *     geom_pair_off[g] (S*S FP64 each) in `distances`/`transitions_constant`.
+ *   chains c: chain_geom[c], kT[c], E_constant (N FP64 at site offset),
+ *     site_energies (S FP64, electrode energies at [N..S)), occupation
+ *     (N bytes, in/out), hops[c], seed.
+ *   outputs: time[c], electrode_occupation (P int64 per chain, overwritten),
+ *     status[c].
+ * lanes_per_chain 0 = choose automatically.
+ */
+int kmc_run_batch_host(int32_t n_geoms, const int32_t *geom_N, const int32_t *geom_P,
+                       const double *geom_nu, const double *geom_I0, const double *geom_R,
+                       const int64_t *geom_pair_off, const double *distances,
+                       const double *transitions_constant, int32_t n_chains,
+                       const int32_t *chain_geom, const double *chain_kT,
+                       const double *E_constant, const double *site_energies,
+                       uint8_t *occupation, const int64_t *hops, uint64_t seed,
+                       int32_t lanes_per_chain, double *time_out,
+                       int64_t *electrode_occupation, int32_t *status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KMC_DN_GB300_H */

@@ -1,0 +1,34 @@
+// kmc_internal.h -- host-side helpers shared by the translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/kmc_dn_gb300.h"
+
+namespace kmc {
+
+// Largest site count the batched engine accepts: keeps the number of pairs
+// A(h) < 2^22 (exact float-reciprocal pair decoding) and the per-chain
+// shared-memory lists within one block.
+constexpr int kMaxSitesF32 = 2048;
+// Largest site count of the plain FP64 kernel.
+constexpr int kMaxSitesF64 = 2048;
+
+// Record an error for kmc_last_error and return its code.
+int fail(int code, const char *fmt, ...);
+int fail_cuda(cudaError_t e, const char *what);
+int ok();
+
+int run_batch(const kmc_batch &b, cudaStream_t st);
+int engine_smem_words(int max_sites);
+int build_table(int N, int P, double nu, double I0, double R, const double *d, const double *tc,
+                float *tab, cudaStream_t st);
+int site_energies(int n_chains, int N, int P, const double *basis, const double *V, double mu,
+                  const double *comp, float *Ec, float *Vel, cudaStream_t st);
+int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_t *occ,
+                 const double *d, const double *Ec, const double *se, const double *tc,
+                 int64_t *eo, int64_t hops, int record, double *traffic, double *oit,
+                 const double *uniforms, uint64_t seed, int32_t *hop_log, double *time_out,
+                 int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st);
+size_t f64_workspace_size(int S);
+
+}  // namespace kmc

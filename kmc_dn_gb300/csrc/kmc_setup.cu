@@ -1,0 +1,142 @@
+// kmc_setup.cu -- per-geometry and per-chain set-up kernels.
+//
+//  build_table    FP64 distances / transitions_constant -> the engine's FP32
+//                 pair table of (L, B) = (log2(nu*tc), I_0 R/d) pairs
+//                 (calc_transitions_constant kmc_dopant_networks.py:824-830;
+//                 the Coulomb term of dE :72-75 / simulation.go:67-68).
+//  site_energies  constant site energies of many chains from the Laplace
+//                 basis fields sampled at the acceptors: the superposition
+//                 sum_e V_e phi_e + mu phi_mu plus donor compensation, which
+//                 replaces one FEniCS solve per voltage vector
+//                 (update_V + calc_E_constant_V_comp, kmc_dopant_networks.py:
+//                 798-821, 865-899).
+//  ex2_peak       microbenchmark of the SFU ex2 rate (the roofline of the
+//                 rate evaluation).
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kmc_common.cuh"
+#include "kmc_internal.h"
+
+namespace kmc {
+namespace {
+
+__global__ void build_table_kernel(int N, int P, double nu, double IR, const double *d,
+                                   const double *tc, float2 *tab)
+{
+    const int S = N + P;
+    const int64_t SS = (int64_t)S * S;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < SS;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = static_cast<int>(k / S), j = static_cast<int>(k - (k / S) * S);
+        const double w = nu * tc[k];
+        const float L = (w > 0.0) ? static_cast<float>(log2(w)) : -INFINITY;
+        const float B = (i < N && j < N && i != j) ? static_cast<float>(IR / d[k]) : 0.0f;
+        tab[k] = make_float2(L, B);
+    }
+}
+
+__global__ void site_energies_kernel(int n_chains, int N, int P, const double *basis,
+                                     const double *V, double mu, const double *comp, float *Ec,
+                                     float *Vel)
+{
+    const int64_t total = (int64_t)n_chains * N;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int c = static_cast<int>(k / N), i = static_cast<int>(k - (int64_t)c * N);
+        double e = 0.0;
+        for (int el = 0; el < P; ++el) e += V[(int64_t)c * P + el] * basis[(int64_t)el * N + i];
+        e += mu * basis[(int64_t)P * N + i];
+        e += comp[i];
+        Ec[k] = static_cast<float>(e);
+    }
+    const int64_t tv = (int64_t)n_chains * P;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < tv;
+         k += (int64_t)gridDim.x * blockDim.x)
+        Vel[k] = static_cast<float>(V[k]);
+}
+
+// Independent ex2 chains, 8 per thread, so the SFU pipe is the limit.
+__global__ void ex2_peak_kernel(int iters, float *sink)
+{
+    float a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = -1.0e-3f * (threadIdx.x + u);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            float y;
+            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a[u]));
+            a[u] = y - 1.0f;
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += a[u];
+    if (s == 12345.0f) sink[threadIdx.x] = s;
+}
+
+}  // namespace
+
+int build_table(int N, int P, double nu, double I0, double R, const double *d, const double *tc,
+                float *tab, cudaStream_t st)
+{
+    const int S = N + P;
+    if (N < 0 || P < 0 || S <= 0 || S > kMaxSitesF32)
+        return fail(KMC_ERR_INVALID, "build_table: bad sizes N=%d P=%d", N, P);
+    if (!d || !tc || !tab) return fail(KMC_ERR_INVALID, "build_table: NULL pointer");
+    const int64_t SS = (int64_t)S * S;
+    const int threads = 256;
+    const int blocks = static_cast<int>((SS + threads - 1) / threads < 4096 ? (SS + threads - 1) / threads : 4096);
+    build_table_kernel<<<blocks, threads, 0, st>>>(N, P, nu, I0 * R, d, tc, reinterpret_cast<float2 *>(tab));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "build_table launch");
+}
+
+int site_energies(int n_chains, int N, int P, const double *basis, const double *V, double mu,
+                  const double *comp, float *Ec, float *Vel, cudaStream_t st)
+{
+    if (n_chains < 0 || N < 0 || P < 0) return fail(KMC_ERR_INVALID, "site_energies: bad sizes");
+    if (!basis || (!V && P > 0) || !comp || !Ec || (!Vel && P > 0))
+        return fail(KMC_ERR_INVALID, "site_energies: NULL pointer");
+    const int64_t total = (int64_t)n_chains * (N > P ? N : P);
+    if (total == 0) return KMC_OK;
+    const int threads = 256;
+    const int blocks = static_cast<int>((total + threads - 1) / threads < 8192 ? (total + threads - 1) / threads : 8192);
+    site_energies_kernel<<<blocks, threads, 0, st>>>(n_chains, N, P, basis, V, mu, comp, Ec, Vel);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "site_energies launch");
+}
+
+}  // namespace kmc
+
+extern "C" int kmc_measure_ex2_rate(double *ex2_per_second)
+{
+    using namespace kmc;
+    if (!ex2_per_second) return fail(KMC_ERR_INVALID, "measure_ex2_rate: NULL output");
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail_cuda(e, "measure_ex2_rate: device query");
+    float *sink = nullptr;
+    e = cudaMalloc(&sink, 1024 * sizeof(float));
+    if (e != cudaSuccess) return fail_cuda(e, "measure_ex2_rate: cudaMalloc");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int threads = 512, blocks = sms * 4, iters = 4096;
+    ex2_peak_kernel<<<blocks, threads>>>(iters, sink);   // warm-up
+    cudaEventRecord(a);
+    ex2_peak_kernel<<<blocks, threads>>>(iters, sink);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess) return fail_cuda(e, "measure_ex2_rate: timing");
+    *ex2_per_second = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+    return KMC_OK;
+}

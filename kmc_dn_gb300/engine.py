@@ -1,0 +1,429 @@
+"""Host side of the hop-loop kernels: device buffers, launches, results.
+
+Device memory and streams come from PyTorch (tensors are only buffers); the
+computation is the CUDA kernels behind the C ABI (``_native``).  Nothing here
+computes hops on the CPU.
+
+* ``simulate_f64``   -- one chain through the plain FP64 kernel (numba
+                        semantics; optional replay stream and hop log).
+* ``Batch``          -- many chains through the batched FP32 engine: pair
+                        tables shared by chains of one geometry, per-chain
+                        state resident on the device, chains binned by size
+                        into launches with their own lanes-per-chain.
+* ``simulate_cuda``  -- keyword-compatible replacement of the reference's
+                        ``_simulate_discrete_record`` / ``callGoSimulation``
+                        (kmc_dopant_networks.py:33-135, goSimulation/
+                        pythonBind.py:49-92) for ``makeSimulation``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import check, lib
+
+__all__ = ["simulate_f64", "TableSpec", "Batch", "simulate_cuda", "superpose", "default_lanes",
+           "make_work_lists", "device"]
+
+
+def device(dev=None):
+    if not torch.cuda.is_available():
+        raise RuntimeError("kmc_dn_gb300 needs a CUDA device: the hop loop runs only as CUDA kernels")
+    return torch.device(dev if dev is not None else "cuda")
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream_handle(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dev(a, dtype, dev):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(dev)
+
+
+# ---------------------------------------------------------------------------
+# plain FP64 single chain
+# ---------------------------------------------------------------------------
+
+def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
+                 transitions_constant, hops, *, electrode_occupation=None, record=False,
+                 uniforms=None, seed=0, hop_log=False, dev=None, stream=None):
+    """Run one chain on the plain FP64 kernel.
+
+    Returns dict(time, occupation, electrode_occupation, traffic,
+    occupations_in_time, hop_log, status).  ``uniforms`` (2*hops values in
+    (0,1)) switches on replay mode."""
+    d = device(dev)
+    S = N + P
+    hops = int(hops)
+    f64 = torch.float64
+    occ = _dev(np.asarray(occupation, dtype=np.uint8).reshape(N), torch.uint8, d)
+    dist = _dev(np.asarray(distances, np.float64).reshape(S, S), f64, d)
+    tc = _dev(np.asarray(transitions_constant, np.float64).reshape(S, S), f64, d)
+    ec = _dev(np.asarray(E_constant, np.float64).reshape(N), f64, d)
+    se = _dev(np.asarray(site_energies, np.float64).reshape(S), f64, d)
+    eo0 = np.zeros(P, np.int64) if electrode_occupation is None else np.asarray(electrode_occupation, np.int64)
+    eo = _dev(eo0.reshape(P), torch.int64, d)
+    traffic = torch.zeros((S, S), dtype=f64, device=d) if record else None
+    oit = torch.zeros(max(N, 1), dtype=f64, device=d) if record else None
+    u = None
+    if uniforms is not None:
+        u = _dev(np.asarray(uniforms, np.float64), f64, d)
+        if u.numel() < 2 * hops:
+            raise ValueError("replay stream shorter than 2*hops")
+    log = torch.zeros(2 * max(hops, 1), dtype=torch.int32, device=d) if hop_log else None
+    t_out = torch.zeros(1, dtype=f64, device=d)
+    st_out = torch.zeros(1, dtype=torch.int32, device=d)
+    L = lib()
+    wsb = L.kmc_simulate_f64_workspace_size(S)
+    ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
+    check(L.kmc_simulate_f64(N, P, float(nu), float(kT), float(I_0), float(R), _ptr(occ), _ptr(dist),
+                             _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), hops, int(bool(record)),
+                             _ptr(traffic), _ptr(oit), _ptr(u), int(seed) & (2**64 - 1), _ptr(log),
+                             _ptr(t_out), _ptr(st_out), _ptr(ws), wsb, _stream_handle(stream)))
+    torch.cuda.synchronize(d)
+    out = dict(time=float(t_out.item()), occupation=occ.cpu().numpy().astype(bool),
+               electrode_occupation=eo.cpu().numpy(), status=int(st_out.item()))
+    out["traffic"] = traffic.cpu().numpy() if record else np.zeros((S, S))
+    out["occupations_in_time"] = oit.cpu().numpy()[:N] if record else np.zeros(N)
+    if hop_log:
+        out["hop_log"] = log.cpu().numpy()[: 2 * hops].reshape(hops, 2)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# batched FP32 engine
+# ---------------------------------------------------------------------------
+
+@dataclass
+class TableSpec:
+    """One geometry instance: the FP64 tables the hop loop reads."""
+    N: int
+    P: int
+    nu: float
+    I_0: float
+    R: float
+    distances: np.ndarray
+    transitions_constant: np.ndarray
+
+    @property
+    def S(self):
+        return self.N + self.P
+
+
+def default_lanes(S):
+    """Lanes per chain by size (the autotuner refines this per workload)."""
+    if S <= 48:
+        return 8
+    if S <= 96:
+        return 16
+    return 32
+
+
+_REANCHOR = 1024
+
+
+def make_work_lists(S_c, hops, lanes=None):
+    """Bin chains by lanes-per-chain and pack each bin into warp items.
+
+    Returns a list of (G, work, order, max_sites): ``work`` holds 32/G chain
+    ids per warp item (-1 pads the last item); chains are ordered by size,
+    then hop budget (both descending) so that the chains sharing a warp have
+    similar per-hop work and similar lifetimes."""
+    S_c = np.asarray(S_c, np.int64).reshape(-1)
+    hops = np.broadcast_to(np.asarray(hops, np.int64), S_c.shape)
+    if lanes is None:
+        lane_of = np.array([default_lanes(int(s)) for s in S_c], np.int32)
+    elif callable(lanes):
+        lane_of = np.array([int(lanes(int(s))) for s in S_c], np.int32)
+    else:
+        lane_of = np.full(S_c.shape[0], int(lanes), np.int32)
+    bad = set(lane_of.tolist()) - {4, 8, 16, 32}
+    if bad:
+        raise ValueError(f"lanes per chain must be 4, 8, 16 or 32, got {sorted(bad)}")
+    out = []
+    for G in sorted(set(lane_of.tolist())):
+        idx = np.flatnonzero(lane_of == G)
+        order = idx[np.lexsort((-hops[idx], -S_c[idx]))]
+        cpw = 32 // G
+        nw = (len(order) + cpw - 1) // cpw
+        work = np.full(nw * cpw, -1, np.int32)
+        work[: len(order)] = order
+        out.append((int(G), work, order, int(S_c[idx].max())))
+    return out
+
+
+class Batch:
+    """Device-resident chains for the batched FP32 engine.
+
+    tables:      list of TableSpec; chains name one by index.
+    chain_table: (C,) table index per chain.
+    kT:          (C,) temperature per chain.
+    E_constant:  list of (N_c,) arrays, or a (C, N) array when all chains
+                 share N; alternatively pass ``E_constant_dev`` (a float32
+                 CUDA tensor pool) produced by ``superpose``.
+    el_energy:   list of (P_c,) electrode energies, or (C, P).
+    occupation:  list/array of initial occupations.
+    hops:        (C,) hop budget per chain.
+    streams:     (C,) RNG stream ids (default: chain index); seed keys them.
+    record:      _native.RECORD_NONE / RECORD_NUMBA / RECORD_GO.
+    lanes:       None (by size class), an int for every chain, or a callable
+                 S -> lanes.
+    """
+
+    def __init__(self, tables: Sequence[TableSpec], chain_table, kT, E_constant=None,
+                 el_energy=None, occupation=None, hops=None, *, streams=None, seed=0,
+                 record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
+                 replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR):
+        self.dev = device(dev)
+        d = self.dev
+        self.tables = list(tables)
+        ct = np.asarray(chain_table, np.int32).reshape(-1)
+        self.n = n = ct.shape[0]
+        self.chain_table = ct
+        Ns = np.array([t.N for t in self.tables], np.int32)
+        Ps = np.array([t.P for t in self.tables], np.int32)
+        if np.any(Ps > 64):
+            raise ValueError("the engine supports at most 64 electrodes")
+        self.N_c = Ns[ct]
+        self.P_c = Ps[ct]
+        self.S_c = self.N_c + self.P_c
+        self.record = int(record)
+        self.seed = int(seed) & (2**64 - 1)
+        self.reanchor = int(reanchor)
+        self.warps_per_block = int(warps_per_block)
+
+        # tables -> FP32 (L, B) on device
+        tab_off = np.zeros(len(self.tables), np.int64)
+        off = 0
+        for i, t in enumerate(self.tables):
+            tab_off[i] = off
+            off += 2 * t.S * t.S
+        self.tab_LB = torch.empty(max(off, 2), dtype=torch.float32, device=d)
+        L = lib()
+        sh = _stream_handle()
+        for i, t in enumerate(self.tables):
+            dd = _dev(np.asarray(t.distances, np.float64).reshape(t.S, t.S), torch.float64, d)
+            tc = _dev(np.asarray(t.transitions_constant, np.float64).reshape(t.S, t.S), torch.float64, d)
+            check(L.kmc_build_table(t.N, t.P, float(t.nu), float(t.I_0), float(t.R), _ptr(dd), _ptr(tc),
+                                    C.c_void_p(self.tab_LB.data_ptr() + 4 * int(tab_off[i])), sh))
+            torch.cuda.current_stream().synchronize()
+        self.tab_N = _dev(Ns, torch.int32, d)
+        self.tab_P = _dev(Ps, torch.int32, d)
+        self.tab_off = _dev(tab_off, torch.int64, d)
+
+        # per-chain offsets
+        self.site_off = np.concatenate([[0], np.cumsum(self.N_c)[:-1]]).astype(np.int64)
+        self.el_off = np.concatenate([[0], np.cumsum(self.P_c)[:-1]]).astype(np.int64)
+        self.pair_off = np.concatenate([[0], np.cumsum(self.S_c.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+        nsite = int(self.N_c.sum())
+        nel = int(self.P_c.sum())
+
+        def pool(vals, total, dtype, np_dtype):
+            if isinstance(vals, np.ndarray) and vals.ndim == 2:
+                flat = vals.astype(np_dtype).reshape(-1)
+            else:
+                flat = np.concatenate([np.asarray(v, np_dtype).reshape(-1) for v in vals]) if total else np.zeros(0, np_dtype)
+            if flat.shape[0] != total:
+                raise ValueError(f"pool size {flat.shape[0]} != {total}")
+            return _dev(flat if total else np.zeros(1, np_dtype), dtype, d)
+
+        self.E_constant = E_constant_dev if E_constant_dev is not None else pool(E_constant, nsite, torch.float32, np.float32)
+        self.el_energy = el_energy_dev if el_energy_dev is not None else pool(el_energy, nel, torch.float32, np.float32)
+        self.occupation = pool(occupation, nsite, torch.uint8, np.uint8)
+        self.chain_tab_d = _dev(ct, torch.int32, d)
+        self.kT = _dev(np.broadcast_to(np.asarray(kT, np.float32), (n,)), torch.float32, d)
+        self.site_off_d = _dev(self.site_off, torch.int64, d)
+        self.el_off_d = _dev(self.el_off, torch.int64, d)
+        self.pair_off_d = _dev(self.pair_off, torch.int64, d)
+        self.electrode_occupation = torch.zeros(max(nel, 1), dtype=torch.int64, device=d)
+        self.time = torch.zeros(n, dtype=torch.float64, device=d)
+        self.hops_done = torch.zeros(n, dtype=torch.int64, device=d)
+        self.hops_total = _dev(np.broadcast_to(np.asarray(hops, np.int64), (n,)), torch.int64, d)
+        sid = np.arange(n, dtype=np.uint64) if streams is None else np.asarray(streams, np.uint64)
+        self.stream_ids = _dev(sid.view(np.int64), torch.int64, d)
+        self.status = torch.zeros(n, dtype=torch.int32, device=d)
+        self.n_pairs = torch.zeros(n, dtype=torch.int64, device=d)
+        if self.record:
+            self.occ_time = torch.zeros(max(nsite, 1), dtype=torch.float64, device=d)
+            self.occ_since = torch.zeros(max(nsite, 1), dtype=torch.float64, device=d)
+            self.traffic = torch.zeros(max(int((self.S_c.astype(np.int64) ** 2).sum()), 1),
+                                       dtype=torch.int32, device=d)
+        else:
+            self.occ_time = self.occ_since = self.traffic = None
+        self.replay = self.replay_off = None
+        if replay is not None:
+            rows = [np.asarray(r, np.float64).reshape(-1) for r in replay]
+            roff = np.concatenate([[0], np.cumsum([r.shape[0] for r in rows])[:-1]]).astype(np.int64)
+            self.replay = _dev(np.concatenate(rows), torch.float64, d)
+            self.replay_off = _dev(roff, torch.int64, d)
+        self.cancel = None
+        self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
+
+    # -- work lists --------------------------------------------------------
+    def _make_bins(self, lanes, hops):
+        bins = []
+        for G, work, order, smax in make_work_lists(self.S_c, hops, lanes):
+            bins.append(dict(G=G, n_work=len(work) // (32 // G), work=_dev(work, torch.int32, self.dev),
+                             max_sites=smax, chains=order))
+        return bins
+
+    def _struct(self, bin_, seg):
+        b = _native.KmcBatch()
+        b.n_tables = len(self.tables)
+        b.max_sites = bin_["max_sites"]
+        b.tab_N, b.tab_P, b.tab_off, b.tab_LB = (self.tab_N.data_ptr(), self.tab_P.data_ptr(),
+                                                 self.tab_off.data_ptr(), self.tab_LB.data_ptr())
+        b.n_chains = self.n
+        b.lanes_per_chain = bin_["G"]
+        b.chain_tab = self.chain_tab_d.data_ptr()
+        b.chain_kT = self.kT.data_ptr()
+        b.chain_site_off = self.site_off_d.data_ptr()
+        b.chain_el_off = self.el_off_d.data_ptr()
+        b.chain_pair_off = self.pair_off_d.data_ptr()
+        b.E_constant = self.E_constant.data_ptr()
+        b.el_energy = self.el_energy.data_ptr()
+        b.occupation = self.occupation.data_ptr()
+        b.electrode_occupation = self.electrode_occupation.data_ptr()
+        b.time = self.time.data_ptr()
+        b.hops_done = self.hops_done.data_ptr()
+        b.hops_total = self.hops_total.data_ptr()
+        b.stream = self.stream_ids.data_ptr()
+        b.status = self.status.data_ptr()
+        b.n_pairs = self.n_pairs.data_ptr()
+        if self.record:
+            b.occ_time, b.occ_since, b.traffic = (self.occ_time.data_ptr(), self.occ_since.data_ptr(),
+                                                  self.traffic.data_ptr())
+        b.work = bin_["work"].data_ptr()
+        b.n_work = bin_["n_work"]
+        b.record = self.record
+        b.reanchor = self.reanchor
+        b.warps_per_block = self.warps_per_block
+        b.max_hops_per_launch = int(seg)
+        b.seed = self.seed
+        if self.replay is not None:
+            b.replay, b.replay_off = self.replay.data_ptr(), self.replay_off.data_ptr()
+        if self.cancel is not None:
+            b.cancel = self.cancel
+        return b
+
+    def launch(self, max_hops_per_launch=None, stream=None):
+        """One launch per size bin (same stream): advance every chain by up
+        to max_hops_per_launch hops (a multiple of the re-anchor period)."""
+        seg = max_hops_per_launch
+        if seg is None:
+            seg = int(self.hops_total.max().item()) if self.n else 1
+        seg = max(self.reanchor, ((int(seg) + self.reanchor - 1) // self.reanchor) * self.reanchor)
+        L = lib()
+        sh = _stream_handle(stream)
+        for bin_ in self._bins:
+            b = self._struct(bin_, seg)
+            check(L.kmc_run_batch(C.byref(b), sh))
+        return self
+
+    def run(self, stream=None):
+        self.launch(None, stream)
+        return self
+
+    def results(self):
+        """Copy results to the host: dict of numpy arrays (ragged per chain
+        lists for occupations and electrode counts)."""
+        torch.cuda.synchronize(self.dev)
+        eo = self.electrode_occupation.cpu().numpy()
+        occ = self.occupation.cpu().numpy()
+        out = dict(time=self.time.cpu().numpy(), status=self.status.cpu().numpy(),
+                   hops_done=self.hops_done.cpu().numpy(), n_pairs=self.n_pairs.cpu().numpy())
+        out["electrode_occupation"] = [eo[o:o + p] for o, p in zip(self.el_off, self.P_c)]
+        out["occupation"] = [occ[o:o + n].astype(bool) for o, n in zip(self.site_off, self.N_c)]
+        if self.record:
+            ot = self.occ_time.cpu().numpy()
+            tr = self.traffic.cpu().numpy()
+            out["occ_time"] = [ot[o:o + n] for o, n in zip(self.site_off, self.N_c)]
+            out["traffic"] = [tr[o:o + s * s].reshape(s, s) for o, s in zip(self.pair_off, self.S_c)]
+        return out
+
+    def currents(self):
+        """electrode_occupation / time per chain, as (C, P) when P is uniform."""
+        r = self.results()
+        cur = [e / t if t > 0 else np.full(e.shape, np.nan) for e, t in zip(r["electrode_occupation"], r["time"])]
+        if len(set(self.P_c.tolist())) == 1:
+            return np.array(cur)
+        return cur
+
+
+def superpose(basis, comp, voltages, mu=0.0, dev=None, stream=None):
+    """Constant site energies of many chains on one geometry, on the device:
+    returns (E_constant float32 (C*N,), el_energy float32 (C*P,))."""
+    d = device(dev)
+    basis = np.asarray(basis, np.float64)
+    V = np.asarray(voltages, np.float64)
+    C_, P = V.shape
+    N = basis.shape[1]
+    b = _dev(basis, torch.float64, d)
+    v = _dev(V, torch.float64, d)
+    cp = _dev(np.asarray(comp, np.float64), torch.float64, d)
+    ec = torch.empty(max(C_ * N, 1), dtype=torch.float32, device=d)
+    ve = torch.empty(max(C_ * P, 1), dtype=torch.float32, device=d)
+    check(lib().kmc_site_energies(C_, N, P, _ptr(b), _ptr(v), float(mu), _ptr(cp), _ptr(ec), _ptr(ve),
+                                  _stream_handle(stream)))
+    return ec, ve
+
+
+# ---------------------------------------------------------------------------
+# keyword-compatible replacement for the reference's hop-loop functions
+# ---------------------------------------------------------------------------
+
+def simulate_cuda(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation, distances,
+                  E_constant, site_energies, transitions_constant, transitions=None,
+                  problist=None, electrode_occupation=None, hops=100000, record=False,
+                  goSpecificFunction=None, prune_threshold=0.0, precision="fp32", seed=None,
+                  record_convention="numba", lanes=None):
+    """Drop-in for ``_simulate_discrete_record(**args)`` (and for
+    ``callGoSimulation`` when called with ``goSpecificFunction``) inside
+    ``kmc_dn.makeSimulation`` (kmc_dopant_networks.py:544-619).
+
+    Returns ``(time, occupation, electrode_occupation, traffic,
+    occupations_in_time)``; ``occupation`` is the final state and
+    ``electrode_occupation`` the per-electrode hole count of this run.
+    precision "fp64" runs the plain FP64 kernel (the numba loop's
+    arithmetic), "fp32" the batched engine with one chain."""
+    N, P = int(N_acceptors), int(N_electrodes)
+    hops = int(hops)
+    if seed is None:
+        seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64))
+    occ0 = np.asarray(occupation, dtype=bool).reshape(N)
+    if precision == "fp64":
+        r = simulate_f64(N, P, nu, kT, I_0, R, occ0, distances, E_constant, site_energies,
+                         transitions_constant, hops, record=record, seed=seed)
+        if r["status"] != 0:
+            raise _native.KmcError(r["status"], "hop loop stopped: no allowed transition or non-finite total rate")
+        return (r["time"], r["occupation"], r["electrode_occupation"], r["traffic"],
+                r["occupations_in_time"])
+    if precision != "fp32":
+        raise ValueError("precision must be 'fp32' or 'fp64'")
+    S = N + P
+    spec = TableSpec(N, P, float(nu), float(I_0), float(R), np.asarray(distances, np.float64),
+                     np.asarray(transitions_constant, np.float64))
+    rec = 0
+    if record:
+        rec = _native.RECORD_GO if record_convention == "go" else _native.RECORD_NUMBA
+    se = np.asarray(site_energies, np.float64).reshape(S)
+    b = Batch([spec], [0], [float(kT)], [np.asarray(E_constant, np.float64)], [se[N:]], [occ0.astype(np.uint8)],
+              [hops], seed=seed, record=rec, lanes=lanes)
+    b.run()
+    r = b.results()
+    if r["status"][0] != 0:
+        raise _native.KmcError(int(r["status"][0]), "hop loop stopped: no allowed transition or non-finite total rate")
+    traffic = r["traffic"][0].astype(np.float64) if record else np.zeros((S, S))
+    oit = r["occ_time"][0] if record else np.zeros(N)
+    return (float(r["time"][0]), r["occupation"][0], r["electrode_occupation"][0].astype(np.int64),
+            traffic, oit)

@@ -1,0 +1,53 @@
+"""The C-ABI library loads on the CPU host and exports every function that
+include/kmc_dn_gb300.h declares (no compute calls: no GPU here)."""
+import ctypes as C
+import os
+import re
+
+from conftest import REPO
+
+
+def declared_functions():
+    src = open(os.path.join(REPO, "include", "kmc_dn_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:int|size_t|double|void)\s+\**\s*(kmc_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "kmc_simulate_f64" in names and "kmc_run_batch" in names and "kmc_last_error" in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    lib = C.CDLL(os.path.join(REPO, "kmc_dn_gb300", "libkmc_dn_gb300.so"))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(engine_lib):
+    from kmc_dn_gb300 import _native
+    assert set(declared_functions()) <= set(_native.EXPORTED)
+
+
+def test_error_channel_without_gpu(engine_lib):
+    """Argument validation happens before any CUDA call and reports through
+    kmc_last_error."""
+    from kmc_dn_gb300 import _native
+    L = _native.lib()
+    rc = L.kmc_build_table(-1, 0, 1.0, 1.0, 1.0, None, None, None, None)
+    assert rc == _native.KMC_ERR_INVALID
+    code, msg = _native.last_error()
+    assert code == rc and "bad sizes" in msg
+    assert L.kmc_run_batch(None, None) == _native.KMC_ERR_INVALID
+    assert L.kmc_version() >= 100
+
+
+def test_struct_layout_matches_header():
+    """ctypes mirror of struct kmc_batch: field order and names as in the header."""
+    from kmc_dn_gb300._native import KmcBatch
+    src = open(os.path.join(REPO, "include", "kmc_dn_gb300.h")).read()
+    body = src[src.index("typedef struct kmc_batch {"):src.index("} kmc_batch;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"(\w+)\s*;", body)
+    assert fields == [f[0] for f in KmcBatch._fields_]

@@ -1,0 +1,231 @@
+"""GPU parity: the CUDA kernels against the oracle and the reference's golden
+replays.  Every test here runs on the device through the C ABI."""
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden
+from kmc_dn_gb300.rng import replay_uniforms
+
+pytestmark = pytest.mark.gpu
+
+REPLAYS = golden_files("replay_*.npz")
+
+
+def _f64(g, hops=None, uniforms=None, seed=0, record=True, hop_log=True, occupation=None):
+    from kmc_dn_gb300.engine import simulate_f64
+    hops = int(g["hops"]) if hops is None else hops
+    return simulate_f64(int(g["N"]), int(g["P"]), float(g["nu"]), float(g["kT"]), float(g["I_0"]),
+                        float(g["R"]), g["occupation"] if occupation is None else occupation,
+                        g["distances"], g["E_constant"], g["site_energies"], g["transitions_constant"],
+                        hops, record=record, uniforms=uniforms, seed=seed, hop_log=hop_log)
+
+
+@pytest.mark.parametrize("path", REPLAYS, ids=lambda p: p.split("replay_")[-1][:-4])
+def test_f64_kernel_replays_reference(engine_lib, path):
+    """Bit-exact hop sequence of the reference's own loop on the same stream
+    (1e5 hops for the two long cases)."""
+    g = load_golden(path)
+    hops = int(g["hops"])
+    u = replay_uniforms(int(g["seed"]), 2 * hops)
+    r = _f64(g, uniforms=u)
+    assert r["status"] == 0
+    log = r["hop_log"]
+    ref = g["hop_log"].astype(np.int32)
+    mism = np.flatnonzero(np.any(log != ref, axis=1))
+    assert mism.size == 0, f"first divergence at hop {mism[0]} of {hops}"
+    np.testing.assert_array_equal(r["electrode_occupation"], g["final_electrode_occupation"])
+    np.testing.assert_array_equal(r["occupation"].astype(np.uint8), g["final_occupation"])
+    np.testing.assert_array_equal(r["traffic"], g["traffic"])
+    assert abs(r["time"] - float(g["time"])) <= 1e-11 * abs(float(g["time"]))
+    np.testing.assert_allclose(r["occupations_in_time"], g["occupations_in_time"], rtol=1e-11)
+
+
+def test_f64_kernel_matches_oracle_fresh_seeds(engine_lib, oracle_mod):
+    from kmc_dn_gb300 import workloads
+    net = workloads.plain_network(3)
+    for seed in (21, 22):
+        hops = 5000
+        u = replay_uniforms(seed, 2 * hops)
+        g = dict(N=net.N, P=net.P, nu=net.nu, kT=net.kT, I_0=net.I_0, R=net.R,
+                 occupation=net.occupation.astype(np.uint8), distances=net.distances,
+                 E_constant=net.E_constant(), site_energies=net.site_energies(),
+                 transitions_constant=net.transitions_constant)
+        r = _f64(g, hops=hops, uniforms=u)
+        o = oracle_mod.numba_replay(net.N, net.P, net.nu, net.kT, net.I_0, net.R, g["occupation"],
+                                    net.distances, g["E_constant"], g["site_energies"],
+                                    net.transitions_constant, u, record=True)
+        np.testing.assert_array_equal(r["hop_log"], o["hop_log"])
+        assert abs(r["time"] - o["time"]) <= 1e-11 * o["time"]
+
+
+def test_f64_philox_mode_runs(engine_lib):
+    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+    a = _f64(g, hops=2000, seed=5, record=False, hop_log=True)
+    b = _f64(g, hops=2000, seed=5, record=False, hop_log=True)
+    c = _f64(g, hops=2000, seed=6, record=False, hop_log=True)
+    assert a["status"] == 0
+    np.testing.assert_array_equal(a["hop_log"], b["hop_log"])     # deterministic per seed
+    assert np.any(a["hop_log"] != c["hop_log"])
+
+
+def _batch_one(g, hops, uniforms=None, record=0, lanes=8, seed=0):
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    N, P = int(g["N"]), int(g["P"])
+    spec = TableSpec(N, P, float(g["nu"]), float(g["I_0"]), float(g["R"]), g["distances"],
+                     g["transitions_constant"])
+    se = np.asarray(g["site_energies"], np.float64)
+    b = Batch([spec], [0], [float(g["kT"])], [g["E_constant"]], [se[N:]], [g["occupation"]], [hops],
+              seed=seed, record=record, lanes=lanes,
+              replay=[uniforms] if uniforms is not None else None)
+    b.run()
+    return b.results()
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+def test_f32_engine_replay_agrees_where_margins_allow(engine_lib, oracle_mod, lanes):
+    """Fed the same stream, the FP32 engine picks the reference's pair on every
+    hop whose event uniform is further than 1e-4 (relative) from a cumulative
+    boundary; the sequences may part only after the first closer call."""
+    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+    hops = 4000
+    u = replay_uniforms(int(g["seed"]), 2 * hops)
+    o = oracle_mod.numba_replay(int(g["N"]), int(g["P"]), float(g["nu"]), float(g["kT"]),
+                                float(g["I_0"]), float(g["R"]), g["occupation"], g["distances"],
+                                g["E_constant"], g["site_energies"], g["transitions_constant"], u,
+                                hops=hops, record=True)
+    close = np.flatnonzero(o["margins"] < 1e-4)
+    safe = int(close[0]) if close.size else hops
+    assert safe > 50
+    r = _batch_one(g, safe, uniforms=u, record=1, lanes=lanes)
+    assert r["status"][0] == 0
+    # the final state after `safe` hops equals the oracle's state after `safe` hops
+    o2 = oracle_mod.numba_replay(int(g["N"]), int(g["P"]), float(g["nu"]), float(g["kT"]),
+                                 float(g["I_0"]), float(g["R"]), g["occupation"], g["distances"],
+                                 g["E_constant"], g["site_energies"], g["transitions_constant"], u,
+                                 hops=safe, record=True)
+    np.testing.assert_array_equal(r["occupation"][0], o2["occupation"].astype(bool))
+    np.testing.assert_array_equal(r["electrode_occupation"][0], o2["electrode_occupation"])
+    np.testing.assert_array_equal(r["traffic"][0], o2["traffic"].astype(np.int32))
+    assert abs(r["time"][0] - o2["time"]) <= 1e-4 * o2["time"]
+    np.testing.assert_allclose(r["occ_time"][0], o2["occupations_in_time"], rtol=1e-4,
+                               atol=1e-4 * o2["time"])
+
+
+def test_f32_engine_same_alone_and_in_the_mix(engine_lib):
+    """A chain's result does not depend on which other chains share its launch."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    nets = [workloads.plain_network(s) for s in (1, 2)]
+    specs = [TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant) for n in nets]
+    hops = 6000
+
+    def run(chains):
+        b = Batch(specs, [c[0] for c in chains], [1.0] * len(chains),
+                  [nets[c[0]].E_constant() for c in chains],
+                  [nets[c[0]].electrodes[:, 3] for c in chains],
+                  [nets[c[0]].occupation.astype(np.uint8) for c in chains],
+                  [c[1] for c in chains], streams=[c[2] for c in chains], seed=77, lanes=8)
+        b.run()
+        return b.results()
+    alone = run([(0, hops, 5)])
+    mix = run([(1, 3000, 9), (0, 1000, 4), (0, hops, 5), (1, hops, 11), (0, 2500, 3)])
+    assert alone["status"][0] == 0
+    assert mix["time"][2] == alone["time"][0]
+    np.testing.assert_array_equal(mix["electrode_occupation"][2], alone["electrode_occupation"][0])
+    np.testing.assert_array_equal(mix["occupation"][2], alone["occupation"][0])
+
+
+def test_f32_engine_split_launches_identical(engine_lib):
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = workloads.plain_network(4)
+    spec = TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant)
+
+    def mk():
+        return Batch([spec], [0, 0], [1.0, 1.0], [n.E_constant()] * 2, [n.electrodes[:, 3]] * 2,
+                     [n.occupation.astype(np.uint8)] * 2, [8192, 8192], seed=3, lanes=8, record=2)
+    a = mk().launch(8192).results()
+    b = mk()
+    for _ in range(4):
+        b.launch(2048)
+    b = b.results()
+    np.testing.assert_array_equal(a["time"], b["time"])
+    for k in ("electrode_occupation", "occupation", "traffic", "occ_time"):
+        for x, y in zip(a[k], b[k]):
+            np.testing.assert_array_equal(x, y)
+    assert list(b["hops_done"]) == [8192, 8192]
+
+
+def test_f32_engine_statistics_vs_fp64_oracle(engine_lib, oracle_mod):
+    """Electrode currents of the FP32 engine agree with the FP64 oracle within
+    3 sigma of their Monte Carlo error (independent seeds on both sides)."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = workloads.plain_network(0)
+    hops = 100_000
+    reps_gpu, reps_cpu = 256, 16
+    spec = TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant)
+    b = Batch([spec], [0] * reps_gpu, [1.0] * reps_gpu, [n.E_constant()] * reps_gpu,
+              [n.electrodes[:, 3]] * reps_gpu, [n.occupation.astype(np.uint8)] * reps_gpu,
+              [hops] * reps_gpu, seed=1234, lanes=8)
+    b.run()
+    r = b.results()
+    assert np.all(r["status"] == 0)
+    cur32 = np.array([e / t for e, t in zip(r["electrode_occupation"], r["time"])])
+    cur64 = []
+    for s in range(reps_cpu):
+        u = replay_uniforms(9000 + s, 2 * hops)
+        o = oracle_mod.numba_replay(n.N, n.P, n.nu, n.kT, n.I_0, n.R, n.occupation.astype(np.uint8),
+                                    n.distances, n.E_constant(), n.site_energies(),
+                                    n.transitions_constant, u, record=False)
+        cur64.append(o["electrode_occupation"] / o["time"])
+    cur64 = np.array(cur64)
+    m32, m64 = cur32.mean(0), cur64.mean(0)
+    sig = np.sqrt(cur32.var(0, ddof=1) / reps_gpu + cur64.var(0, ddof=1) / reps_cpu)
+    z = np.abs(m32 - m64) / sig
+    assert np.all(z < 3.0), (z, m32, m64)
+
+
+def test_run_batch_host_matches_device_batch(engine_lib):
+    """The host-buffer C entry point gives the device-buffer path's results."""
+    import ctypes as C
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300._native import lib, check
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = workloads.plain_network(2)
+    nc, hops, seed = 24, 3000, 99
+    V = np.random.default_rng(0).uniform(-1, 1, (nc, n.P))
+    ec = np.concatenate([n.E_constant(v) for v in V])
+    se = np.concatenate([np.concatenate([np.zeros(n.N), v]) for v in V])
+    occ = np.tile(n.occupation.astype(np.uint8), nc)
+    t_out = np.zeros(nc)
+    eo = np.zeros(nc * n.P, np.int64)
+    st = np.zeros(nc, np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(lib().kmc_run_batch_host(1, p(np.array([n.N], np.int32)), p(np.array([n.P], np.int32)),
+                                   p(np.array([n.nu])), p(np.array([n.I_0])), p(np.array([n.R])),
+                                   p(np.array([0], np.int64)), p(np.ascontiguousarray(n.distances)),
+                                   p(np.ascontiguousarray(n.transitions_constant)), nc,
+                                   p(np.zeros(nc, np.int32)), p(np.ones(nc)), p(ec), p(se), p(occ),
+                                   p(np.full(nc, hops, np.int64)), seed, 8, p(t_out), p(eo), p(st)))
+    spec = TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant)
+    b = Batch([spec], [0] * nc, [1.0] * nc, [n.E_constant(v) for v in V], list(V),
+              [n.occupation.astype(np.uint8)] * nc, [hops] * nc, seed=seed, lanes=8)
+    r = b.run().results()
+    np.testing.assert_array_equal(st, 0)
+    np.testing.assert_array_equal(t_out, r["time"])
+    np.testing.assert_array_equal(eo.reshape(nc, n.P), np.array(r["electrode_occupation"]))
+
+
+def test_no_allowed_transition_reports_status(engine_lib):
+    """A closed single-site system has no allowed hop: the chain stops with
+    KMC_ERR_NONFINITE instead of producing NaN times (the reference divides
+    by a zero total rate)."""
+    from kmc_dn_gb300.engine import Batch, TableSpec, simulate_f64
+    from kmc_dn_gb300._native import KMC_ERR_NONFINITE
+    d = np.zeros((1, 1))
+    tc = np.zeros((1, 1))
+    r = simulate_f64(1, 0, 1.0, 1.0, 1.0, 1.0, [1], d, [0.0], [0.0], tc, 10)
+    assert r["status"] == KMC_ERR_NONFINITE
+    b = Batch([TableSpec(1, 0, 1.0, 1.0, 1.0, d, tc)], [0], [1.0], [[0.0]], [[]], [[1]], [10], lanes=4)
+    assert b.run().results()["status"][0] == KMC_ERR_NONFINITE

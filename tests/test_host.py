@@ -1,0 +1,43 @@
+"""Host-side logic that needs no GPU."""
+import numpy as np
+import pytest
+
+from kmc_dn_gb300.engine import make_work_lists, default_lanes
+from kmc_dn_gb300.rng import replay_uniforms
+
+
+def test_work_lists_cover_every_chain_once():
+    rng = np.random.default_rng(0)
+    S = rng.integers(14, 212, 1000)
+    hops = rng.integers(1, 10**6, 1000)
+    seen = []
+    for G, work, order, smax in make_work_lists(S, hops):
+        assert len(work) % (32 // G) == 0
+        ids = work[work >= 0]
+        assert np.all([default_lanes(int(S[i])) == G for i in ids])
+        assert smax == S[ids].max()
+        # within a bin chains are sorted by size then hops (descending)
+        key = list(zip(-S[ids], -hops[ids]))
+        assert key == sorted(key)
+        seen.extend(ids.tolist())
+    assert sorted(seen) == list(range(1000))
+
+
+def test_work_lists_reject_bad_lanes():
+    with pytest.raises(ValueError):
+        make_work_lists([38], [10], lanes=6)
+
+
+def test_replay_stream_open_interval_and_reproducible():
+    u = replay_uniforms(123, 100000)
+    assert np.all(u > 0) and np.all(u < 1)
+    np.testing.assert_array_equal(u, replay_uniforms(123, 100000))
+    assert abs(u.mean() - 0.5) < 0.01
+
+
+def test_native_library_missing_fails_loudly(tmp_path, monkeypatch):
+    from kmc_dn_gb300 import _native
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "nope.so"))
+    monkeypatch.setattr(_native, "_LIB", None)
+    with pytest.raises(_native.NativeLibraryError):
+        _native.lib()

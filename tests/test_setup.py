@@ -1,0 +1,85 @@
+"""Set-up numerics against the reference's own fixtures (thesis_indrek/tests
+.kmc files, copied to tests/golden/fixtures_*.npz by make_golden.py)."""
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden
+from kmc_dn_gb300 import geometry as geo
+from kmc_dn_gb300.laplace import default_cells, solve_basis_fields
+
+FIXTURES = golden_files("fixtures_*.npz")
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: p.split("fixtures_")[-1][:-4])
+def test_eV_constant_matches_fenics(path):
+    """FD basis fields + P1 interpolation reproduce the FEniCS potential at
+    every acceptor (boundary-segment ends and the diagonal orientation
+    included)."""
+    f = load_golden(path)
+    worst = 0.0
+    for k in range(len(f["N"])):
+        xdim, ydim, res = float(f["xdim"][k]), float(f["ydim"][k]), float(f["res"][k])
+        el = f["electrodes"][k]
+        bf = solve_basis_fields(xdim, ydim, el[:, :2], default_cells(xdim, res), default_cells(ydim, res))
+        ev = bf.sample(f["acceptors"][k][:, :2])
+        V = el[:, 3] @ ev[:-1] + float(f["mu"][k]) * ev[-1]
+        err = np.max(np.abs(V - f["eV_constant"][k])) / np.max(np.abs(f["eV_constant"][k]))
+        worst = max(worst, err)
+    assert worst < 1e-11, worst
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: p.split("fixtures_")[-1][:-4])
+def test_tables_match_fixture(path):
+    f = load_golden(path)
+    for k in range(len(f["N"])):
+        acc, el = f["acceptors"][k], f["electrodes"][k]
+        d = geo.site_distances(acc, el)
+        np.testing.assert_array_equal(d, f["distances"][k])
+        tc = geo.transitions_constant(d, float(f["nu"][k]), float(f["ab"][k]))
+        np.testing.assert_allclose(tc, f["transitions_constant"][k], rtol=1e-15, atol=1e-300)
+        comp = geo.compensation(acc, f["donors"][k], float(f["I_0"][k]), float(f["R"][k]))
+        np.testing.assert_allclose(comp, f["comp_constant"][k], rtol=1e-13)
+        R, dim = geo.dimensionless_R(int(f["N"][k]), float(f["xdim"][k]), float(f["ydim"][k]),
+                                     float(f["zdim"][k]))
+        assert dim == 2 and R == float(f["R"][k])
+
+
+def test_default_cells_floor_division():
+    assert default_cells(1.0, 0.01) == 99
+    assert default_cells(20.0, 0.2) == 99
+
+
+def test_1d_basis_is_linear():
+    bf = solve_basis_fields(1.0, 0.0, np.array([[0.0, 0.0], [1.0, 0.0]]), 100)
+    x = np.array([[0.25, 0, 0], [0.5, 0, 0]])
+    v = bf.sample(x)
+    np.testing.assert_allclose(v[0], [0.75, 0.5])
+    np.testing.assert_allclose(v[1], [0.25, 0.5])
+    np.testing.assert_allclose(v[2], [0.0, 0.0])
+
+
+def test_superposition_linearity():
+    from kmc_dn_gb300 import workloads
+    n = workloads.plain_network(5)
+    V1, V2 = np.linspace(-1, 1, 8), np.cos(np.arange(8))
+    np.testing.assert_allclose(n.eV(V1 + 2 * V2), n.eV(V1) + 2 * n.eV(V2), rtol=1e-12, atol=1e-12)
+
+
+def test_total_energy_detailed_balance():
+    """dE of every allowed hop equals the change of total_energy (with the
+    constant site term that includes compensation) -- the identity behind
+    the Boltzmann checks."""
+    from kmc_dn_gb300 import workloads
+    n = workloads.plain_network(6)
+    N, P = n.N, n.P
+    Ec = n.E_constant(np.zeros(P))
+    IR = n.I_0 * n.R
+    occ = n.occupation.copy()
+    E = Ec - IR * np.array([sum(1 / n.distances[i, j] for j in range(N) if j != i and not occ[j])
+                            for i in range(N)])
+    H0 = geo.total_energy(occ, n.distances, Ec, n.I_0, n.R)
+    for i in np.flatnonzero(occ)[:5]:
+        for j in np.flatnonzero(~occ)[:3]:
+            o2 = occ.copy(); o2[i] = False; o2[j] = True
+            dE = E[j] - E[i] - IR / n.distances[i, j]
+            assert abs((geo.total_energy(o2, n.distances, Ec, n.I_0, n.R) - H0) - dE) < 1e-9
