@@ -1,0 +1,358 @@
+"""Benchmark: hops/s of the batched FP32 engine on the homogeneous ensemble.
+
+Workload (one step): 4096 independent chains on the N=30, M=3, 20x20,
+8-electrode network (kmc_dn_gb300.workloads.plain_network), each chain with
+its own U[-1,1] voltage vector and RNG stream, 1e6 hops per chain, run as
+one graph-captured launch of the engine.  Inputs are synthetic and seeded
+(the reference publishes no dataset for this path).
+
+Printed (rank 0, one JSON line): whole-job hops/s with inputs resident on
+the device (`value`), the same through the host-buffer C entry point
+(`e2e`), the plain single-chain FP64 kernel's hops/s on the same network
+(`fp64_single_chain`), the roofline of the dominant kernel against the
+measured ex2 (SFU) rate, the CPU baseline (the C restatement of the
+reference's Go loop on host threads), and SM clocks sampled during the
+timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+For N > 1 (torchrun, one rank per GPU) every rank runs its own 4096 chains
+(weak scaling, no collective on the data path); time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_CHAINS = 4096
+HOPS = 1_000_000
+METRIC = "hops/s on 1 GB300: batched FP32 vs plain FP64 at ≤1% current error; p99 lat"
+WORKLOAD = "homogeneous ensemble: 4096 chains x 1e6 hops, N=30 M=3 P=8, 20x20, FP32 rates / FP64 clock"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(seed, n_chains, chain_offset=0):
+    from kmc_dn_gb300 import workloads
+    net, V = workloads.homogeneous_ensemble(n_chains + chain_offset, seed)
+    return net, V[chain_offset:chain_offset + n_chains]
+
+
+def cpu_baseline(net, V, threads, hops, n_chains, budget_s=20.0):
+    """The C restatement of the reference's Go hop loop (no state memo),
+    FP32 rates, O(N) energy updates, FP64 clock, one chain per host thread
+    task, on a bounded sample of the workload's chains."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as orc
+    N, P = net.N, net.P
+    occ = np.tile(net.occupation.astype(np.uint8), (n_chains, 1))
+    ec = np.stack([net.E_constant(v) for v in V[:n_chains]])
+    se = np.stack([np.concatenate([np.zeros(N), v]) for v in V[:n_chains]])
+    # calibrate: one short run to size the sample near budget_s
+    t0 = time.perf_counter()
+    orc.go_chains(N, P, net.nu, net.kT, net.I_0, net.R, occ[:threads], net.distances, ec[:threads],
+                  se[:threads], net.transitions_constant, 2000, seed=7, threads=threads)
+    per_hop = (time.perf_counter() - t0) / (2000 * threads) * threads   # s per hop per thread
+    h = int(min(hops, max(2000, budget_s / max(per_hop, 1e-9) * threads / n_chains)))
+    t0 = time.perf_counter()
+    times, eo, na = orc.go_chains(N, P, net.nu, net.kT, net.I_0, net.R, occ, net.distances, ec, se,
+                                  net.transitions_constant, h, seed=11, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n_chains * h / dt, "unit": "hops/s", "cores": threads, "kind": "port",
+            "sample": f"{n_chains} chains x {h} hops of the workload (C restatement of the "
+                      f"reference's Go simulate loop, no memo), {dt:.1f} s wall"}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    net, V = build_workload(args.seed, N_CHAINS)
+    threads = os.cpu_count() or 1
+    n_chains = 256
+    from kmc_dn_gb300 import workloads  # noqa: F401
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(net, V, threads, HOPS, n_chains, budget_s=max(2.0, 60.0 / max(1, args.steps + args.warmup)))
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": "hops/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "hops": HOPS, "parallelism": "none (CPU)",
+                       "l2": "n/a (CPU)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "hops/s", "cores": threads, "kind": "port",
+                             "sample": r["sample"] + " per step"},
+            "e2e": {"value": v, "unit": "hops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--hops", type=int, default=HOPS)
+    ap.add_argument("--chains", type=int, default=N_CHAINS)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--warps-per-block", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from kmc_dn_gb300 import _native
+    from kmc_dn_gb300.engine import Batch, TableSpec, superpose, simulate_f64
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    n_chains, hops = args.chains, args.hops
+    net, V = build_workload(args.seed, n_chains, chain_offset=rank * n_chains)
+    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    ec_dev, vel_dev = superpose(net.basis, net.comp, V, net.mu, dev=dev)
+    occ0 = np.tile(net.occupation.astype(np.uint8), (n_chains, 1))
+    lanes = args.lanes if args.lanes else None
+    b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT), None, None, occ0,
+              np.full(n_chains, hops), streams=np.arange(n_chains) + rank * n_chains, seed=args.seed + 1,
+              lanes=lanes, warps_per_block=args.warps_per_block, dev=dev, E_constant_dev=ec_dev,
+              el_energy_dev=vel_dev)
+    occ_init = b.occupation.clone()
+    stream = torch.cuda.Stream(device=dev)
+
+    def reset():
+        b.occupation.copy_(occ_init)
+        b.time.zero_()
+        b.hops_done.zero_()
+        b.electrode_occupation.zero_()
+        b.n_pairs.zero_()
+
+    # graph-captured step: state reset + one engine launch per size bin
+    with torch.cuda.stream(stream):
+        reset()
+        b.launch(hops, stream=stream)
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        reset()
+        b.launch(hops, stream=stream)
+    launches_per_step = len(b._bins)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2
+
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize(dev)
+    r0 = b.results()
+    assert np.all(r0["status"] == 0), "engine reported a chain error"
+    pairs_per_step = int(np.sum(r0["n_pairs"]))
+    hops_per_step = int(np.sum(r0["hops_done"]))
+    assert hops_per_step == n_chains * hops
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    step_ms = []
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)                      # evict L2 between steps (outside the events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - wall0
+    clocks = clk.summary()
+    total_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * hops_per_step * args.steps / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+
+    # roofline: allowed pairs (one ex2 each) per launch / launch time vs measured ex2 rate
+    peak = C.c_double(0)
+    _native.check(_native.lib().kmc_measure_ex2_rate(C.byref(peak)))
+    achieved = pairs_per_step / (ms_per_step * 1e-3)
+    traffic = None
+    tpath = os.path.join(HERE, "profiles", "engine_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
+        except (ValueError, OSError):
+            traffic = None
+
+    out = None
+    if rank == 0:
+        # plain single-chain FP64 kernel on the same network (Philox stream)
+        f64_hops = 100_000
+        se = net.site_energies(V[0])
+        simulate_f64(net.N, net.P, net.nu, net.kT, net.I_0, net.R, net.occupation, net.distances,
+                     net.E_constant(V[0]), se, net.transitions_constant, 2000, seed=1, dev=dev)
+        t0 = time.perf_counter()
+        r64 = simulate_f64(net.N, net.P, net.nu, net.kT, net.I_0, net.R, net.occupation, net.distances,
+                           net.E_constant(V[0]), se, net.transitions_constant, f64_hops, seed=2, dev=dev)
+        f64_rate = f64_hops / (time.perf_counter() - t0)
+        assert r64["status"] == 0
+
+        # e2e: the host-buffer C entry point, copies in and out inside the call
+        e2e = None
+        if not args.no_e2e:
+            e2e = run_e2e(net, V, hops, args.seed + 1, lanes or 0)
+
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            cpu = cpu_baseline(net, V, os.cpu_count() or 1, hops, min(256, n_chains))
+
+        out = {"metric": METRIC, "value": value, "unit": "hops/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "n_chains": n_chains, "hops": hops,
+                          "lanes_per_chain": b._bins[0]["G"], "warps_per_block": args.warps_per_block,
+                          "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                          "l2": "flushed between steps (512 MB write)"},
+               "fp64_single_chain": {"value": f64_rate, "unit": "hops/s", "hops": f64_hops,
+                                     "workload": "1 chain, same network, plain FP64 kernel"},
+               "ratio_vs_fp64_single_chain": value / world / f64_rate,
+               "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
+                            "unit": "Gexp/s", "frac": achieved / peak.value, "traffic": traffic,
+                            "peak_source": "ex2.approx throughput measured live (kmc_measure_ex2_rate)",
+                            "work": "allowed pairs A(h) summed over all hops of a launch, one ex2 each"},
+               "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "gpu_launches": launches_per_step * args.steps,
+               "wall_s": wall}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(net, V, hops, seed, lanes):
+    """Same workload through kmc_run_batch_host: host FP64 inputs copied to
+    the device, the run, results copied back, all inside the timed call."""
+    from kmc_dn_gb300._native import lib, check
+    n = V.shape[0]
+    N, P = net.N, net.P
+    ec = np.ascontiguousarray(np.concatenate([net.E_constant(v) for v in V]))
+    se = np.ascontiguousarray(np.concatenate([np.concatenate([np.zeros(N), v]) for v in V]))
+    occ = np.ascontiguousarray(np.tile(net.occupation.astype(np.uint8), n))
+    hops_a = np.full(n, hops, np.int64)
+    kT = np.full(n, net.kT)
+    cg = np.zeros(n, np.int32)
+    t_out = np.zeros(n)
+    eo = np.zeros(n * P, np.int64)
+    st = np.zeros(n, np.int32)
+    d = np.ascontiguousarray(net.distances)
+    tc = np.ascontiguousarray(net.transitions_constant)
+    gN, gP = np.array([N], np.int32), np.array([P], np.int32)
+    gnu, gI, gR, goff = np.array([net.nu]), np.array([net.I_0]), np.array([net.R]), np.zeros(1, np.int64)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    L = lib()
+
+    def call():
+        occ[:] = np.tile(net.occupation.astype(np.uint8), n)
+        check(L.kmc_run_batch_host(1, p(gN), p(gP), p(gnu), p(gI), p(gR), p(goff), p(d), p(tc), n, p(cg),
+                                   p(kT), p(ec), p(se), p(occ), p(hops_a), seed, lanes, p(t_out), p(eo), p(st)))
+    call()   # warm-up (allocator pools, module load)
+    t0 = time.perf_counter()
+    reps = 2
+    for _ in range(reps):
+        call()
+    dt = (time.perf_counter() - t0) / reps
+    assert np.all(st == 0)
+    # bytes kmc_run_batch_host copies each call (its FP32 staging of the
+    # energies, the FP64 geometry tables, per-chain parameters and offsets)
+    G = lanes or (8 if N + P <= 48 else 16 if N + P <= 96 else 32)
+    n_work = (n + 32 // G - 1) // (32 // G)
+    h2d = (d.nbytes + tc.nbytes + 4 * n * N + 4 * n * P + 4 * n + 4 + 4 + 8 + 4 * n + 8 * n + 8 * n
+           + occ.nbytes + hops_a.nbytes + 8 * n + 4 * n_work * (32 // G))
+    d2h = t_out.nbytes + eo.nbytes + occ.nbytes + st.nbytes
+    return {"value": n * hops / dt, "unit": "hops/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "api": "kmc_run_batch_host (C ABI, host buffers)"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,122 @@
+"""Autotuner for the batched engine's launch shape.
+
+For a size class (sites per chain) it times short runs of the engine on
+synthetic chains of that size for every lanes-per-chain G in {4, 8, 16, 32}
+and warps per block in {2, 4, 8}, on the device at hand, and keeps the
+fastest (hops/s).  Results are cached per (GPU name, size class, number of
+chains) in a JSON file (``KMC_DN_AUTOTUNE_CACHE`` or
+``~/.cache/kmc_dn_gb300/autotune.json``), so a workload is tuned once per
+machine.  ``choose`` returns a ``lanes`` callable for ``Batch``.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+import time
+
+import numpy as np
+
+__all__ = ["tune_size_class", "choose", "size_class", "cache_path", "CANDIDATE_LANES",
+           "CANDIDATE_WARPS"]
+
+CANDIDATE_LANES = (4, 8, 16, 32)
+CANDIDATE_WARPS = (2, 4, 8)
+_CLASS_EDGES = (24, 48, 96, 160, 256, 512, 1024, 2048)
+_LOCK = threading.Lock()
+
+
+def size_class(S):
+    """Upper edge of the size class that S falls in."""
+    for e in _CLASS_EDGES:
+        if S <= e:
+            return e
+    return _CLASS_EDGES[-1]
+
+
+def cache_path():
+    return os.environ.get("KMC_DN_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "kmc_dn_gb300", "autotune.json"))
+
+
+def _load():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d):
+    p = cache_path()
+    try:
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        tmp = p + f".tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, p)
+    except OSError:
+        pass
+
+
+def _key(gpu, sc, n_chains):
+    # chain counts in powers of two: occupancy is what changes with them
+    return f"{gpu}|S<={sc}|C~{1 << max(0, int(np.ceil(np.log2(max(n_chains, 1)))))}"
+
+
+def tune_size_class(S, n_chains, hops=4096, seed=0, dev=None, verbose=False):
+    """Time every (G, warps per block) for chains of S sites; return the best
+    as dict(G, warps_per_block, hops_per_s, table)."""
+    import torch
+    from . import workloads
+    from .engine import Batch, TableSpec
+    N = max(1, S - 8)
+    P = S - N
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = float(np.sqrt(N / workloads.DENSITY))
+    net = workloads.make_network(rng, N, max(0, int(round(0.1 * N))), L, L,
+                                 workloads.perimeter_electrodes(L, P), voltages=rng.uniform(-1, 1, P),
+                                 I_0=50.0, cells=40)
+    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    table = []
+    for G in CANDIDATE_LANES:
+        for W in CANDIDATE_WARPS:
+            b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT),
+                      np.tile(net.E_constant(), (n_chains, 1)), np.tile(net.electrodes[:, 3], (n_chains, 1)),
+                      np.tile(net.occupation.astype(np.uint8), (n_chains, 1)), np.full(n_chains, 2 * hops),
+                      seed=seed, lanes=G, warps_per_block=W, dev=dev)
+            b.launch(1024)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.launch(hops)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            rate = n_chains * hops / dt
+            table.append((G, W, rate))
+            if verbose:
+                print(f"S={S} C={n_chains} G={G} W={W}: {rate:.3e} hops/s")
+    G, W, rate = max(table, key=lambda r: r[2])
+    return dict(G=int(G), warps_per_block=int(W), hops_per_s=float(rate),
+                table=[list(map(float, r)) for r in table])
+
+
+def choose(S_values, n_chains, dev=None, tune=True):
+    """Per-size-class lanes for a workload: a callable S -> G (cached)."""
+    import torch
+    gpu = torch.cuda.get_device_name(dev) if torch.cuda.is_available() else "none"
+    classes = sorted({size_class(int(s)) for s in np.atleast_1d(S_values)})
+    with _LOCK:
+        cache = _load()
+        picked = {}
+        for sc in classes:
+            k = _key(gpu, sc, n_chains)
+            if k not in cache and tune:
+                cache[k] = tune_size_class(sc, n_chains, dev=dev)
+                _save(cache)
+            picked[sc] = cache[k]["G"] if k in cache else None
+    from .engine import default_lanes
+
+    def lanes(S):
+        g = picked.get(size_class(S))
+        return g if g else default_lanes(S)
+    return lanes

@@ -384,9 +384,17 @@ int launch(const kmc_batch &b, cudaStream_t st)
     const int wpb = b.warps_per_block;
     const size_t smem = static_cast<size_t>(wpb) * CPW * chain_smem_words(b.max_sites) * 4;
     if (smem > 227 * 1024) return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds 227 KB", smem, b.max_sites, G, wpb);
-    cudaError_t e = cudaFuncSetAttribute(f32_engine_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(engine)");
+    // Raise the dynamic shared-memory limit only when a launch needs more than
+    // any before it, so launches under stream capture make no attribute calls
+    // once a first launch has run.
+    static int configured = 0;
+    cudaError_t e;
+    if (static_cast<int>(smem) > configured) {
+        e = cudaFuncSetAttribute(f32_engine_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem));
+        if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(engine)");
+        configured = static_cast<int>(smem);
+    }
     const int grid = (b.n_work + wpb - 1) / wpb;
     if (grid <= 0) return KMC_OK;
     f32_engine_kernel<G><<<grid, wpb * 32, smem, st>>>(b);

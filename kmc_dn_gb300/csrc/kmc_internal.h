@@ -31,4 +31,28 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
                  int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st);
 size_t f64_workspace_size(int S);
 
+// Host-buffer batch run (FP64 host inputs, copies in/out, synchronous).
+struct HostRun {
+    int32_t n_geoms;
+    const int32_t *geom_N, *geom_P;
+    const double *geom_nu, *geom_I0, *geom_R;
+    const int64_t *geom_pair_off;
+    const double *distances, *transitions_constant;
+    int32_t n_chains;
+    const int32_t *chain_geom;
+    const double *chain_kT, *E_constant, *site_energies;
+    uint8_t *occupation;
+    const int64_t *hops;
+    const uint64_t *streams;        // NULL: chain index
+    uint64_t seed;
+    int32_t lanes_per_chain;
+    int32_t record;                 // KMC_RECORD_*
+    double *time_out;
+    int64_t *electrode_occupation;  // overwritten
+    int32_t *status;
+    double *traffic_out;            // record: S*S per chain, accumulated
+    double *occ_time_out;           // record: N per chain, accumulated
+};
+int host_run(const HostRun &h);
+
 }  // namespace kmc

@@ -27,8 +27,8 @@ import torch
 from . import _native
 from ._native import check, lib
 
-__all__ = ["simulate_f64", "TableSpec", "Batch", "simulate_cuda", "superpose", "default_lanes",
-           "make_work_lists", "device"]
+__all__ = ["simulate_f64", "TableSpec", "Batch", "simulate_cuda", "simulate_go", "superpose",
+           "default_lanes", "make_work_lists", "device", "prune"]
 
 
 def device(dev=None):
@@ -263,6 +263,9 @@ class Batch:
         self.replay = self.replay_off = None
         if replay is not None:
             rows = [np.asarray(r, np.float64).reshape(-1) for r in replay]
+            need = 2 * np.broadcast_to(np.asarray(hops, np.int64), (n,))
+            if len(rows) != n or any(r.shape[0] < k for r, k in zip(rows, need)):
+                raise ValueError("replay needs one stream of at least 2*hops uniforms per chain")
             roff = np.concatenate([[0], np.cumsum([r.shape[0] for r in rows])[:-1]]).astype(np.int64)
             self.replay = _dev(np.concatenate(rows), torch.float64, d)
             self.replay_off = _dev(roff, torch.int64, d)
@@ -427,3 +430,46 @@ def simulate_cuda(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation, d
     oit = r["occ_time"][0] if record else np.zeros(N)
     return (float(r["time"][0]), r["occupation"][0], r["electrode_occupation"][0].astype(np.int64),
             traffic, oit)
+
+
+def prune(transitions_constant, threshold):
+    """Zero the pairs a pruned Go run leaves out of its transition list:
+    ``tc <= threshold * max(tc)`` (simulation.go:199-215).  A zero constant
+    gives a zero rate, so the pair can never be selected."""
+    tc = np.array(transitions_constant, dtype=np.float64, copy=True)
+    if threshold and threshold > 0:
+        tc[tc <= threshold * tc.max()] = 0.0
+    return tc
+
+
+def simulate_go(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation, distances,
+                E_constant, site_energies, transitions_constant, transitions=None, problist=None,
+                electrode_occupation=None, hops=100000, record=False,
+                goSpecificFunction="wrapperSimulateRecord", prune_threshold=0.0, seed=None,
+                lanes=None):
+    """Drop-in for ``callGoSimulation`` (goSimulation/pythonBind.py:49-92)
+    with the Go library's semantics on the FP32 engine: the chain starts with
+    every acceptor empty (simulationWrapper.go:134-141), the caller's
+    occupation comes back unchanged (pythonBind.py:84), record counts net
+    traffic and credits occupancy before each hop (simulation.go:309-317).
+    Returns (time, occupation, electrode_occupation[, traffic,
+    average_occupation])."""
+    N, P = int(N_acceptors), int(N_electrodes)
+    if seed is None:
+        seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64))
+    thr = prune_threshold if goSpecificFunction == "wrapperSimulatePruned" else 0.0
+    tc = prune(transitions_constant, thr)
+    S = N + P
+    se = np.asarray(site_energies, np.float64).reshape(S)
+    spec = TableSpec(N, P, float(nu), float(I_0), float(R), np.asarray(distances, np.float64), tc)
+    b = Batch([spec], [0], [float(kT)], [np.asarray(E_constant, np.float64)], [se[N:]],
+              [np.zeros(N, np.uint8)], [int(hops)], seed=seed,
+              record=_native.RECORD_GO if record else _native.RECORD_NONE, lanes=lanes)
+    r = b.run().results()
+    if r["status"][0] != 0:
+        raise _native.KmcError(int(r["status"][0]), "hop loop stopped: no allowed transition or non-finite total rate")
+    occ_out = np.array([int(x) for x in np.asarray(occupation).reshape(N)])
+    eo = r["electrode_occupation"][0].astype(np.int64)
+    if not record:
+        return float(r["time"][0]), occ_out, eo
+    return (float(r["time"][0]), occ_out, eo, r["traffic"][0].astype(np.float64), r["occ_time"][0])

@@ -7,10 +7,14 @@ import re
 from conftest import REPO
 
 
-def declared_functions():
-    src = open(os.path.join(REPO, "include", "kmc_dn_gb300.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:int|size_t|double|void)\s+\**\s*(kmc_\w+)\s*\(", src, flags=re.M)
+def declared_functions(header=None):
+    """Function names declared in include/*.h (or one header)."""
+    import glob
+    paths = [os.path.join(REPO, "include", header)] if header else glob.glob(os.path.join(REPO, "include", "*.h"))
+    names = []
+    for path in paths:
+        src = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+        names += re.findall(r"^\s*(?:int|int64_t|size_t|double|void)\s+\**\s*(\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
@@ -27,7 +31,15 @@ def test_library_exports_every_declared_symbol(engine_lib):
 
 def test_python_binding_covers_header(engine_lib):
     from kmc_dn_gb300 import _native
-    assert set(declared_functions()) <= set(_native.EXPORTED)
+    assert set(declared_functions("kmc_dn_gb300.h")) <= set(_native.EXPORTED)
+
+
+def test_go_compat_names_exported(engine_lib):
+    """The Go library's export names, so the reference's ctypes bridge can
+    load this library in place of libSimulation.so."""
+    names = declared_functions("kmc_goslice_compat.h")
+    assert {"wrapperSimulate", "wrapperSimulateRecord", "wrapperSimulatePruned",
+            "wrapperSimulateRecordPlus", "parallelSimulations"} <= set(names)
 
 
 def test_error_channel_without_gpu(engine_lib):
