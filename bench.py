@@ -218,8 +218,9 @@ def main():
     launches_per_step = len(b._bins)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2
 
-    for _ in range(args.warmup):
-        g.replay()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            g.replay()
     torch.cuda.synchronize(dev)
     r0 = b.results()
     assert np.all(r0["status"] == 0), "engine reported a chain error"
@@ -237,9 +238,10 @@ def main():
             flush.fill_(1.0)                      # evict L2 between steps (outside the events)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            g.replay()
-            e1.record(stream)
+            with torch.cuda.stream(stream):      # replay and events on one stream
+                e0.record(stream)
+                g.replay()
+                e1.record(stream)
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
         torch.cuda.synchronize(dev)

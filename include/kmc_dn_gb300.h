@@ -93,6 +93,13 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
 #define KMC_RECORD_GO 2      /* traffic[f,t] += 1, traffic[t,f] -= 1; occupancy
                                 credited before the hop (simulation.go:309-317) */
 
+/* Where the engine takes L = log2(nu*tc_ij) and B = I_0 R / d_ij from. */
+#define KMC_PAIRS_TABLE 0      /* per-geometry pair table (tab_LB): any tables */
+#define KMC_PAIRS_POSITIONS 1  /* site coordinates (tab_pos): tc = nu*exp(-2d/ab),
+                                  the reference's calc_transitions_constant
+                                  (kmc_dopant_networks.py:824-830); only valid
+                                  when the tables are those of the positions */
+
 /*
  * Launch description of the batched engine.  Every pointer is device
  * memory.  A "table" is one geometry instance: S*S interleaved float pairs
@@ -103,9 +110,11 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
  * entries per chain) and per-pair pools (S*S entries per chain) are indexed
  * by the chain's offsets.
  *
- * The work list assigns chains to warps: item w is 32/G chain ids
- * work[w*(32/G) + s] (-1 = empty slot) run by one warp, G lanes per chain.
- * Chains in one item should have similar size and hop budget.
+ * The work list assigns chains to thread groups.  For G <= 32 lanes per
+ * chain, item w is 32/G chain ids work[w*(32/G) + s] (-1 = empty slot) run
+ * by one warp; for G in {64, 128, 256, 512}, item w is one chain id run by
+ * one block of G threads.  Chains in one item should have similar size and
+ * hop budget.
  *
  * Each launch advances every listed chain by min(hops_total - hops_done,
  * max_hops_per_launch) hops (max_hops_per_launch a multiple of reanchor),
@@ -124,7 +133,7 @@ typedef struct kmc_batch {
     const float *tab_LB;            /* pair tables, 2*S*S floats each          */
     /* chains */
     int32_t n_chains;
-    int32_t lanes_per_chain;        /* G in {4, 8, 16, 32}                     */
+    int32_t lanes_per_chain;        /* G in {4, 8, 16, 32, 64, 128, 256, 512}  */
     const int32_t *chain_tab;       /* [n_chains]                              */
     const float *chain_kT;          /* [n_chains]                              */
     const int64_t *chain_site_off;  /* [n_chains] offset into per-site pools   */
@@ -154,6 +163,12 @@ typedef struct kmc_batch {
     const double *replay;           /* optional 2 uniforms per hop per chain   */
     const int64_t *replay_off;      /* [n_chains] offset into replay           */
     const volatile int32_t *cancel; /* optional host-mapped cancel word        */
+    /* pair rates from coordinates instead of tables (KMC_PAIRS_POSITIONS) */
+    int32_t pair_mode;              /* KMC_PAIRS_TABLE or KMC_PAIRS_POSITIONS  */
+    const float *tab_pos;           /* sites' (x, y, z, 0), 4 floats per site  */
+    const int64_t *tab_pos_off;     /* [n_tables] offset in floats into tab_pos*/
+    const float *tab_coef;          /* [n_tables*4]: -2*log2(e)/ab,
+                                       log2(nu*nu), I_0*R, 0                   */
 } kmc_batch;
 
 /*

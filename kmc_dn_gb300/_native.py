@@ -13,6 +13,7 @@ import threading
 __all__ = ["lib", "check", "KmcError", "NativeLibraryError", "KmcBatch", "LIB_PATH",
            "KMC_OK", "KMC_ERR_INVALID", "KMC_ERR_CUDA", "KMC_ERR_OOM", "KMC_ERR_TIMEOUT",
            "KMC_ERR_NONFINITE", "KMC_ERR_CANCELLED", "RECORD_NONE", "RECORD_NUMBA", "RECORD_GO",
+           "PAIRS_TABLE", "PAIRS_POSITIONS",
            "EXPORTED"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -26,6 +27,7 @@ KMC_ERR_TIMEOUT = -4
 KMC_ERR_NONFINITE = -5
 KMC_ERR_CANCELLED = -6
 RECORD_NONE, RECORD_NUMBA, RECORD_GO = 0, 1, 2
+PAIRS_TABLE, PAIRS_POSITIONS = 0, 1
 
 _vp = C.c_void_p
 _i32, _i64, _u64, _f64, _sz = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_size_t
@@ -55,6 +57,7 @@ class KmcBatch(C.Structure):
         ("work", _vp), ("n_work", _i32), ("record", _i32), ("reanchor", _i32),
         ("warps_per_block", _i32), ("max_hops_per_launch", _i64), ("seed", _u64),
         ("replay", _vp), ("replay_off", _vp), ("cancel", _vp),
+        ("pair_mode", _i32), ("tab_pos", _vp), ("tab_pos_off", _vp), ("tab_coef", _vp),
     ]
 
 

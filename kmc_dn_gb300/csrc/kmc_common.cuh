@@ -45,6 +45,16 @@ __device__ __forceinline__ double u01_from64(uint32_t hi, uint32_t lo)
     return (static_cast<double>(v) + 0.5) * 0x1.0p-53;
 }
 
+// Uniform in (0,1) from 52 random bits with one FP64 operation: the bits
+// fill the mantissa of a double in [1,2) whose lowest bit is forced to 1
+// (so the result is never 0; it is at most 1 - 2^-52), and 1 is subtracted.
+__device__ __forceinline__ double u01_from52(uint32_t hi, uint32_t lo)
+{
+    const double one_two = __hiloint2double(static_cast<int>(0x3FF00000u | (hi >> 12)),
+                                            static_cast<int>(lo | 1u));
+    return one_two - 1.0;
+}
+
 // ---------------------------------------------------------------------------
 // Batched-engine launch description (device pointers).  Mirrors struct
 // kmc_batch of the C ABI; kept as the same layout.

@@ -1,7 +1,8 @@
 // kmc_f32.cu -- batched FP32 hop-loop engine for sm_103a.
 //
-// One chain per group of G lanes (G = 4, 8, 16 or 32; 32/G chains per warp).
-// Per hop, for every chain:
+// A chain is run by a group of threads: a G-lane slice of a warp (G = 4, 8,
+// 16, 32; 32/G chains per warp) for small networks, or a whole thread block
+// (G = 64 .. 512) for large ones.  Per hop, for every chain:
 //
 //  pair phase   The allowed transitions are enumerated in the reference's
 //               row-major (from, to) order over compact lists: sources are
@@ -11,18 +12,22 @@
 //               That is exactly the nonzero part of the reference's dense
 //               S x S rate matrix (predicate kmc_dopant_networks.py:137-163,
 //               simulation.go:40-55), A(h) = h(N-h) + hP + P(N-h) pairs.
-//               Lane g owns the contiguous run [g*M, g*M+M) of the A pairs
-//               and sums its Miller-Abrahams rates in FP32:
+//               Thread g owns the contiguous run [g*M, g*M+M) of the A pairs
+//               and sums their Miller-Abrahams rates in FP32:
 //                   rate = 2^(L_ij - c*max(0, e_j - e_i - B_ij))
-//               with L = log2(nu*tc), B = I_0 R / d (acceptor pairs),
-//               e = energies, c = log2(e)/kT: one ex2 per allowed pair
+//               L = log2(nu*tc), B = I_0 R / d (acceptor pairs), e = site
+//               energies, c = log2(e)/kT: one ex2 per allowed pair
 //               (kmc_dopant_networks.py:69-87, simulation.go:58-80).
-//  selection    The G lane sums are scanned in FP64; the clock advances by
-//               Exp(1)/total accumulated in FP64 (simulation.go:297-298);
+//               L and B come from a pair table (any tables the caller
+//               passes, shared by the chains of one geometry) or, in
+//               positions mode, from the sites' coordinates carried in the
+//               lists (d from one rsqrt; no table traffic).
+//  selection    The per-thread sums are scanned in FP64; the clock advances
+//               by Exp(1)/total accumulated in FP64 (simulation.go:297-298);
 //               the event is the first pair whose cumulative rate reaches
 //               u*total (kmc_dopant_networks.py:106-110): the FP64 compare
-//               picks the lane, then the lane's run is re-evaluated by the
-//               group and scanned relative to that lane's FP64 base.
+//               picks the thread, then that thread's run is re-evaluated by
+//               the group and scanned relative to its FP64 base.
 //  hop          O(N) incremental energy update (makeJump,
 //               simulation.go:107-130), occupancy bits, electrode counters,
 //               optional record (numba or Go convention); every `reanchor`
@@ -32,8 +37,8 @@
 //               from the occupancy bitmask (popc ranks), carrying each
 //               site's scaled energy, ready for the next pair phase.
 //
-// Pair tables are read through the read-only data path (L1/L2 resident for
-// shared geometries).  No tensor cores: nothing here is a contraction.
+// No tensor cores: nothing here is a contraction.  No spin-waits: every
+// loop is bounded by the hop budget or the list sizes.
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -54,9 +59,24 @@ __device__ __forceinline__ float ex2_approx(float x)
     return y;
 }
 
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // k -> (row, col) within the pair enumeration.  Float-reciprocal quotient
-// with one correction step; exact for k < 2^22 (the engine limits S so that
-// A(h) stays below that).
+// with one correction step: with inv within 2^-22 (relative) of 1/T and
+// k < 2^22 the estimate is off by less than one, so the result is exact (the
+// engine limits S so that A(h) stays below 2^22).
 __device__ __forceinline__ void decode_pair(int k, int h, int A1, int T1, int T2, float inv1,
                                             float inv2, int &row, int &col)
 {
@@ -76,73 +96,295 @@ __device__ __forceinline__ void decode_pair(int k, int h, int A1, int T1, int T2
     }
 }
 
-struct ChainSmem {
-    int2 *src;        // [S+1] {site, scaled energy bits}
-    int2 *tgt;        // [S+1]
-    float *E;         // [S]   site energies (acceptors)
-    uint32_t *occw;   // [W]   occupancy bits
-    int *eo;          // [kMaxElectrodes] electrode counters of this launch
+// ---------------------------------------------------------------------------
+// Pair-rate sources
+// ---------------------------------------------------------------------------
+
+// Table mode: records are {site, scaled energy}; (L, B) read from the table.
+struct TablePairs {
+    using Rec = int2;
+    const float2 *tab;
+    int S;
+    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int S_)
+    {
+        tab = reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
+        S = S_;
+    }
+    __device__ __forceinline__ Rec rec(int site, float e) const { return make_int2(site, __float_as_int(e)); }
+    __device__ __forceinline__ float rate(Rec s, Rec t, bool /*acc*/, float cs) const
+    {
+        const float2 lb = __ldg(&tab[s.x * S + t.x]);
+        float x = __int_as_float(t.y) - __int_as_float(s.y);
+        x = fmaf(-cs, lb.y, x);
+        x = fmaxf(x, 0.0f);
+        return ex2_approx(lb.x - x);
+    }
+    // Coulomb term I_0 R / d_jk between acceptors j, k (0 on the diagonal).
+    __device__ __forceinline__ float coulomb(int j, int k) const { return __ldg(&tab[j * S + k]).y; }
 };
 
+// Positions mode: records are {x, y, z, scaled energy}; d from coordinates.
+struct PositionPairs {
+    using Rec = float4;
+    const float4 *pos;
+    float kL, L0, IR;
+    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int /*S*/)
+    {
+        pos = reinterpret_cast<const float4 *>(B.tab_pos + B.tab_pos_off[t_id]);
+        const float4 c = reinterpret_cast<const float4 *>(B.tab_coef)[t_id];
+        kL = c.x;    // -2 log2(e) / ab
+        L0 = c.y;    // log2(nu * nu)
+        IR = c.z;    // I_0 R
+    }
+    __device__ __forceinline__ Rec rec(int site, float e) const
+    {
+        const float4 p = __ldg(&pos[site]);
+        return make_float4(p.x, p.y, p.z, e);
+    }
+    __device__ __forceinline__ float rate(Rec s, Rec t, bool acc, float cs) const
+    {
+        const float dx = t.x - s.x, dy = t.y - s.y, dz = t.z - s.z;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float rs = rsqrt_approx(d2);
+        const float L = fmaf(kL, d2 * rs, L0);
+        float x = t.w - s.w;
+        if (acc) x = fmaf(-cs * IR, rs, x);
+        x = fmaxf(x, 0.0f);
+        return ex2_approx(L - x);
+    }
+    __device__ __forceinline__ float coulomb(int j, int k) const
+    {
+        if (j == k) return 0.0f;
+        const float4 a = __ldg(&pos[j]), b = __ldg(&pos[k]);
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        return IR * rsqrt_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Thread groups: a G-lane slice of a warp, or a whole block
+// ---------------------------------------------------------------------------
+
+template <int G>
+struct WarpGroup {
+    static constexpr int kSize = G;
+    int g;            // rank in the group
+    int sub;          // group index within the warp
+    unsigned mask;
+    __device__ __forceinline__ void init()
+    {
+        const int lane = threadIdx.x & 31;
+        sub = lane / G;
+        g = lane % G;
+        mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (sub * G);
+    }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    // inclusive FP64 scan; sets the exclusive value and the total
+    __device__ __forceinline__ double scan(double v, double &excl, double &tot) const
+    {
+        double x = v;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const double o = __shfl_up_sync(mask, x, d, G);
+            if (g >= d) x += o;
+        }
+        const double e = __shfl_up_sync(mask, x, 1, G);
+        excl = g == 0 ? 0.0 : e;
+        tot = __shfl_sync(mask, x, G - 1, G);
+        return x;
+    }
+    __device__ __forceinline__ float scanf(float v, float &tot) const
+    {
+        float x = v;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const float o = __shfl_up_sync(mask, x, d, G);
+            if (g >= d) x += o;
+        }
+        tot = __shfl_sync(mask, x, G - 1, G);
+        return x;
+    }
+    // lowest / highest rank with p true, or -1
+    __device__ __forceinline__ int first(bool p) const
+    {
+        const unsigned low = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
+        const unsigned b = (__ballot_sync(mask, p) >> (sub * G)) & low;
+        return b ? __ffs(b) - 1 : -1;
+    }
+    __device__ __forceinline__ int last(bool p) const
+    {
+        const unsigned low = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
+        const unsigned b = (__ballot_sync(mask, p) >> (sub * G)) & low;
+        return b ? 31 - __clz(b) : -1;
+    }
+    template <typename V>
+    __device__ __forceinline__ V bcast(V v, int src) const { return __shfl_sync(mask, v, src, G); }
+};
+
+// Block-wide group; its scratch lives in static shared memory.
+template <int T>
+struct BlockGroup {
+    static constexpr int kSize = T;
+    static constexpr int kWarps = T / 32;
+    int g;
+    double *sd;   // [kWarps + 2]
+    int *si;      // [2]
+    __device__ __forceinline__ void init() { g = threadIdx.x; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ double scan(double v, double &excl, double &tot) const
+    {
+        const int lane = g & 31, w = g >> 5;
+        double x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double o = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += o;
+        }
+        if (lane == 31) sd[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            double y = lane < kWarps ? sd[lane] : 0.0;
+#pragma unroll
+            for (int d = 1; d < kWarps; d <<= 1) {
+                const double o = __shfl_up_sync(0xffffffffu, y, d);
+                if (lane >= d) y += o;
+            }
+            if (lane < kWarps) sd[lane] = y;
+        }
+        __syncthreads();
+        const double base = w > 0 ? sd[w - 1] : 0.0;
+        tot = sd[kWarps - 1];
+        __syncthreads();
+        x += base;
+        const double prev = __shfl_up_sync(0xffffffffu, x, 1);
+        excl = lane > 0 ? prev : base;
+        return x;
+    }
+    __device__ float scanf(float v, float &tot) const
+    {
+        const int lane = g & 31, w = g >> 5;
+        float x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float o = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += o;
+        }
+        float *sf = reinterpret_cast<float *>(sd);
+        if (lane == 31) sf[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            float y = lane < kWarps ? sf[lane] : 0.0f;
+#pragma unroll
+            for (int d = 1; d < kWarps; d <<= 1) {
+                const float o = __shfl_up_sync(0xffffffffu, y, d);
+                if (lane >= d) y += o;
+            }
+            if (lane < kWarps) sf[lane] = y;
+        }
+        __syncthreads();
+        const float base = w > 0 ? sf[w - 1] : 0.0f;
+        tot = sf[kWarps - 1];
+        __syncthreads();
+        return x + base;
+    }
+    __device__ int first(bool p) const
+    {
+        if (g == 0) si[0] = 0x7fffffff;
+        __syncthreads();
+        if (p) atomicMin(&si[0], g);
+        __syncthreads();
+        const int r = si[0];
+        __syncthreads();
+        return r == 0x7fffffff ? -1 : r;
+    }
+    __device__ int last(bool p) const
+    {
+        if (g == 0) si[1] = -1;
+        __syncthreads();
+        if (p) atomicMax(&si[1], g);
+        __syncthreads();
+        const int r = si[1];
+        __syncthreads();
+        return r;
+    }
+    template <typename V>
+    __device__ V bcast(V v, int src) const
+    {
+        static_assert(sizeof(V) <= sizeof(double), "bcast slot holds one double");
+        V *slot = reinterpret_cast<V *>(sd + kWarps);
+        if (g == src) *slot = v;
+        __syncthreads();
+        const V r = *slot;
+        __syncthreads();
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Per-chain shared memory
+// ---------------------------------------------------------------------------
+
+template <typename Rec>
+struct ChainSmem {
+    Rec *src;        // [S+1] source records
+    Rec *tgt;        // [S+1] target records
+    int *src_id;     // [S+1] site ids of the sources
+    int *tgt_id;     // [S+1] site ids of the targets
+    float *E;        // [S]   site energies (acceptors)
+    uint32_t *occw;  // [W]   occupancy bits
+    int *eo;         // [kMaxElectrodes] electrode counters of this launch
+};
+
+template <typename Rec>
 __host__ __device__ __forceinline__ int chain_smem_words(int S)
 {
     const int W = (S + 31) / 32;
-    int words = 2 * (S + 1) + 2 * (S + 1) + S + W + kMaxElectrodes;
+    const int rw = static_cast<int>(sizeof(Rec) / 4);
+    const int words = 2 * rw * (S + 1) + 2 * (S + 1) + S + W + kMaxElectrodes;
     return (words + 3) & ~3;
 }
 
-__device__ __forceinline__ ChainSmem carve(uint32_t *base, int S)
+template <typename Rec>
+__device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S)
 {
-    ChainSmem c;
-    c.src = reinterpret_cast<int2 *>(base);
+    ChainSmem<Rec> c;
+    c.src = reinterpret_cast<Rec *>(base);
     c.tgt = c.src + (S + 1);
-    c.E = reinterpret_cast<float *>(c.tgt + (S + 1));
+    c.src_id = reinterpret_cast<int *>(c.tgt + (S + 1));
+    c.tgt_id = c.src_id + (S + 1);
+    c.E = reinterpret_cast<float *>(c.tgt_id + (S + 1));
     c.occw = reinterpret_cast<uint32_t *>(c.E + S);
     c.eo = reinterpret_cast<int *>(c.occw + (S + 31) / 32);
     return c;
 }
 
-// Rate of pair (source record s, target record t): one ex2.
-__device__ __forceinline__ float pair_rate(const float2 *__restrict__ tab, int S, int2 s, int2 t,
-                                           float cs)
+// ---------------------------------------------------------------------------
+// The hop loop of one chain, run by one group
+// ---------------------------------------------------------------------------
+
+template <typename Grp, typename Pairs>
+__device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename Pairs::Rec> sm,
+                          int c)
 {
-    const float2 lb = __ldg(&tab[s.x * S + t.x]);
-    float x = __int_as_float(t.y) - __int_as_float(s.y);
-    x = fmaf(-cs, lb.y, x);
-    x = fmaxf(x, 0.0f);
-    return ex2_approx(lb.x - x);
-}
-
-template <int G>
-__global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
-{
-    constexpr int CPW = 32 / G;
-    extern __shared__ __align__(16) uint32_t smem[];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int sub = lane / G;
-    const int g = lane % G;
-    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (sub * G);
-    const int Smax = B.max_sites;
-    const int item = blockIdx.x * B.warps_per_block + warp;
-    if (item >= B.n_work) return;
-    const int c = B.work[item * CPW + sub];
-    if (c < 0 || c >= B.n_chains) return;   // whole group leaves together
-
-    ChainSmem sm = carve(smem + (warp * CPW + sub) * chain_smem_words(Smax), Smax);
-
+    constexpr int G = Grp::kSize;
+    using Rec = typename Pairs::Rec;
+    const int g = grp.g;
     const int t_id = B.chain_tab[c];
     const int N = B.tab_N[t_id];
     const int P = B.tab_P[t_id];
     const int S = N + P;
-    const float2 *tab = reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
+    if (P > kMaxElectrodes || S > B.max_sites || N < 0) {
+        if (g == 0) B.status[c] = KMC_ERR_INVALID;
+        return;
+    }
+    Pairs pairs;
+    pairs.init(B, t_id, S);
     const int64_t so = B.chain_site_off[c];
     const int64_t eoff = B.chain_el_off[c];
     const float *Ec = B.E_constant + so;
     const float *Vel = B.el_energy + eoff;
     uint8_t *occ_g = B.occupation + so;
-    const float kT = B.chain_kT[c];
-    const float cs = kLog2e / kT;
+    const float cs = kLog2e / B.chain_kT[c];
     const int64_t hops_done0 = B.hops_done[c];
     int64_t todo = B.hops_total[c] - hops_done0;
     if (todo > B.max_hops_per_launch) todo = B.max_hops_per_launch;
@@ -151,10 +393,6 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
     const int record = B.record;
     const int reanchor = B.reanchor > 0 ? B.reanchor : 1024;
     const int W = (N + 31) / 32;
-    if (P > kMaxElectrodes || S > Smax || N < 0) {
-        if (g == 0) B.status[c] = KMC_ERR_INVALID;
-        return;
-    }
 
     // ---- load state ----
     for (int w = g; w < W; w += G) {
@@ -166,7 +404,7 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
         sm.occw[w] = bits;
     }
     for (int e = g; e < P; e += G) sm.eo[e] = 0;
-    __syncwarp(gmask);
+    grp.sync();
     int h = 0;
     for (int w = 0; w < W; ++w) h += __popc(sm.occw[w]);
 
@@ -174,37 +412,40 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
     int64_t hop = hops_done0;
     const int64_t hop_end = hops_done0 + (todo > 0 ? todo : 0);
     int status = KMC_OK;
-    unsigned long long pairs = 0;
+    unsigned long long npairs = 0;
     const double *replay = B.replay ? B.replay + B.replay_off[c] : nullptr;
     double *occ_time = record ? B.occ_time + so : nullptr;
     double *occ_since = record ? B.occ_since + so : nullptr;
     int32_t *traffic = record ? B.traffic + B.chain_pair_off[c] : nullptr;
-    if (record) {
+    if (record)
         for (int j = g; j < N; j += G) occ_since[j] = t;
-    }
 
+    // Philox words: thread g holds the draw of hop rbase + (g mod 32)
     u32x4 rnd{0, 0, 0, 0};
     int64_t rbase = INT64_MIN / 2;
-    bool need_anchor = true;
+    constexpr int RW = G < 32 ? G : 32;   // hops per refill
+    // hops until the next multiple of `reanchor` (anchors fall on absolute
+    // hop indices, so a run split into launches anchors at the same hops)
+    int until_anchor = 0;   // anchor at the launch start as well
+    const int phase0 = static_cast<int>(hop % reanchor);
 
     while (hop < hop_end) {
         if (B.cancel && (hop & 1023) == 0) {
-            // one read per group, broadcast, so the group leaves together
-            const int stop = __shfl_sync(gmask, g == 0 ? *B.cancel : 0, 0, G);
+            const int stop = grp.bcast(g == 0 ? *B.cancel : 0, 0);
             if (stop) { status = KMC_ERR_CANCELLED; break; }
         }
         // ---- (re)anchor energies: E_j = Ec_j - sum_{k empty} B_jk ----
-        if (need_anchor || (hop % reanchor) == 0) {
+        if (until_anchor == 0) {
             for (int j = g; j < N; j += G) {
                 float acc = 0.0f;
-                const float2 *row = tab + j * S;
                 for (int k = 0; k < N; ++k)
-                    if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += __ldg(&row[k]).y;
+                    if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += pairs.coulomb(j, k);
                 sm.E[j] = Ec[j] - acc;
             }
-            need_anchor = false;
-            __syncwarp(gmask);
+            until_anchor = (hop == hops_done0 && phase0 != 0) ? reanchor - phase0 : reanchor;
+            grp.sync();
         }
+        --until_anchor;
         // ---- site phase: rebuild ordered source / target lists ----
         {
             const int z = N - h;
@@ -214,16 +455,18 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
                 while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
                 const uint32_t word = sm.occw[w];
                 const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
-                const int2 rec = make_int2(j, __float_as_int(cs * sm.E[j]));
-                if ((word >> (j & 31)) & 1u) sm.src[below] = rec;
-                else sm.tgt[j - below] = rec;
+                const Rec r = pairs.rec(j, cs * sm.E[j]);
+                if ((word >> (j & 31)) & 1u) { sm.src[below] = r; sm.src_id[below] = j; }
+                else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
             }
             for (int e = g; e < P; e += G) {
-                const int2 rec = make_int2(N + e, __float_as_int(cs * Vel[e]));
-                sm.src[h + e] = rec;
-                sm.tgt[z + e] = rec;
+                const Rec r = pairs.rec(N + e, cs * Vel[e]);
+                sm.src[h + e] = r;
+                sm.src_id[h + e] = N + e;
+                sm.tgt[z + e] = r;
+                sm.tgt_id[z + e] = N + e;
             }
-            __syncwarp(gmask);
+            grp.sync();
         }
         // ---- pair phase ----
         const int z = N - h;
@@ -231,71 +474,83 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
         const int A1 = h * T1;
         const int A = A1 + P * T2;
         if (A <= 0) { status = KMC_ERR_NONFINITE; break; }
-        const float inv1 = T1 > 0 ? 1.0f / T1 : 0.0f;
-        const float inv2 = T2 > 0 ? 1.0f / T2 : 0.0f;
+        const float inv1 = T1 > 0 ? rcp_approx(static_cast<float>(T1)) : 0.0f;
+        const float inv2 = T2 > 0 ? rcp_approx(static_cast<float>(T2)) : 0.0f;
         const int M = (A + G - 1) / G;
         float lsum = 0.0f;
         {
+            // The thread's run is walked as U contiguous sub-runs in lock
+            // step: U independent load -> rate -> sum chains per iteration.
+            constexpr int U = 4;
             const int kb = g * M;
             const int ke = min(kb + M, A);
             if (kb < ke) {
-                int row, col;
-                decode_pair(kb, h, A1, T1, T2, inv1, inv2, row, col);
-                int Tcur = row < h ? T1 : T2;
-                int2 sr = sm.src[row];
-                for (int k = kb; k < ke; ++k) {
-                    lsum += pair_rate(tab, S, sr, sm.tgt[col], cs);
-                    if (++col == Tcur) {
-                        col = 0;
-                        ++row;
-                        Tcur = row < h ? T1 : T2;
-                        sr = sm.src[row];
+                const int m = (ke - kb + U - 1) / U;
+                int row[U], col[U], Tc[U], left[U];
+                bool sa[U];
+                Rec sr[U];
+                float acc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int s0 = kb + u * m;
+                    left[u] = max(0, min(m, ke - s0));
+                    acc[u] = 0.0f;
+                    row[u] = col[u] = 0;
+                    if (left[u] > 0) decode_pair(s0, h, A1, T1, T2, inv1, inv2, row[u], col[u]);
+                    sa[u] = row[u] < h;
+                    Tc[u] = sa[u] ? T1 : T2;
+                    sr[u] = sm.src[row[u]];
+                }
+                for (int it = 0; it < m; ++it) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (it < left[u]) {
+                            acc[u] += pairs.rate(sr[u], sm.tgt[col[u]], sa[u] && col[u] < z, cs);
+                            if (++col[u] == Tc[u]) {
+                                col[u] = 0;
+                                ++row[u];
+                                sa[u] = row[u] < h;
+                                Tc[u] = sa[u] ? T1 : T2;
+                                sr[u] = sm.src[row[u]];
+                            }
+                        }
                     }
                 }
+                lsum = ((acc[0] + acc[1]) + acc[2]) + acc[3];
             }
         }
-        pairs += static_cast<unsigned long long>(A);
+        npairs += static_cast<unsigned long long>(A);
         // ---- uniforms for this hop ----
         double u_ev;
         float e1;
         if (replay) {
-            const double u1 = replay[2 * hop], u2 = replay[2 * hop + 1];
-            e1 = -log1pf(-static_cast<float>(u1));
-            u_ev = u2;
+            e1 = -log1pf(-static_cast<float>(replay[2 * hop]));
+            u_ev = replay[2 * hop + 1];
         } else {
-            if (hop - rbase >= G) {
+            if (hop - rbase >= RW) {
                 rbase = hop;
-                const uint64_t ctr = static_cast<uint64_t>(hop + g);
+                const uint64_t ctr = static_cast<uint64_t>(hop + (g & 31));
                 rnd = philox4x32_10(u32x4{static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
-                                          static_cast<uint32_t>(stream),
-                                          static_cast<uint32_t>(stream >> 32)},
+                                          static_cast<uint32_t>(stream), static_cast<uint32_t>(stream >> 32)},
                                     k0, k1);
             }
             const int ri = static_cast<int>(hop - rbase);
-            const uint32_t w0 = __shfl_sync(gmask, rnd.x, ri, G);
-            const uint32_t w1 = __shfl_sync(gmask, rnd.y, ri, G);
-            const uint32_t w2 = __shfl_sync(gmask, rnd.z, ri, G);
-            e1 = -logf(u01_from32(w0));
-            u_ev = u01_from64(w1, w2);
+            const uint32_t w0 = grp.bcast(rnd.x, ri);
+            const uint32_t w1 = grp.bcast(rnd.y, ri);
+            const uint32_t w2 = grp.bcast(rnd.z, ri);
+            e1 = -__logf(u01_from32(w0));
+            u_ev = u01_from52(w1, w2);
         }
-        // ---- FP64 scan of the lane sums ----
-        double v = static_cast<double>(lsum);
-#pragma unroll
-        for (int d = 1; d < G; d <<= 1) {
-            const double o = __shfl_up_sync(gmask, v, d, G);
-            if (g >= d) v += o;
-        }
-        const double tot = __shfl_sync(gmask, v, G - 1, G);
+        // ---- FP64 scan of the per-thread sums ----
+        double excl, tot;
+        const double incl = grp.scan(static_cast<double>(lsum), excl, tot);
         if (!(tot > 0.0) || !(tot < 1.0e300)) { status = KMC_ERR_NONFINITE; break; }
         const double target = u_ev * tot;
-        const unsigned shift = static_cast<unsigned>(sub * G);
-        const unsigned lowG = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
-        const unsigned hitL = (__ballot_sync(gmask, v >= target) >> shift) & lowG;
-        const int L = hitL ? (__ffs(hitL) - 1) : (G - 1);
-        const double excl = __shfl_up_sync(gmask, v, 1, G);
-        const double baseL = __shfl_sync(gmask, g == 0 ? 0.0 : excl, L, G);
+        int L = grp.first(incl >= target);
+        if (L < 0) L = G - 1;
+        const double baseL = grp.bcast(excl, L);
         float rem = static_cast<float>(target - baseL);
-        // ---- re-evaluate lane L's run and find the event ----
+        // ---- re-evaluate thread L's run and find the event ----
         int chosen = -1, last_pos = -1;
         {
             const int kb = L * M;
@@ -306,39 +561,35 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
                 if (k < ke) {
                     int row, col;
                     decode_pair(k, h, A1, T1, T2, inv1, inv2, row, col);
-                    r = pair_rate(tab, S, sm.src[row], sm.tgt[col], cs);
+                    r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
                 }
-                float q = r;
-#pragma unroll
-                for (int d = 1; d < G; d <<= 1) {
-                    const float o = __shfl_up_sync(gmask, q, d, G);
-                    if (g >= d) q += o;
-                }
+                float ctot;
+                const float q = grp.scanf(r, ctot);
                 const bool pos = (k < ke) && (r > 0.0f);
-                const unsigned hit = (__ballot_sync(gmask, pos && q >= rem) >> shift) & lowG;
-                const unsigned pm = (__ballot_sync(gmask, pos) >> shift) & lowG;
-                if (hit) { chosen = kc + __ffs(hit) - 1; break; }
-                if (pm) last_pos = kc + 31 - __clz(pm);
-                rem -= __shfl_sync(gmask, q, G - 1, G);
+                const int hit = grp.first(pos && q >= rem);
+                if (hit >= 0) { chosen = kc + hit; break; }
+                const int lp = grp.last(pos);
+                if (lp >= 0) last_pos = kc + lp;
+                rem -= ctot;
             }
         }
         if (chosen < 0) chosen = last_pos;
         if (chosen < 0) { status = KMC_ERR_NONFINITE; break; }
         int row, col;
         decode_pair(chosen, h, A1, T1, T2, inv1, inv2, row, col);
-        const int from = sm.src[row].x;
-        const int to = sm.tgt[col].x;
+        const int from = sm.src_id[row];
+        const int to = sm.tgt_id[col];
         // ---- clock ----
         const float dt = e1 * __frcp_rn(static_cast<float>(tot));
         const double t_before = t;
         t += static_cast<double>(dt);
-        __syncwarp(gmask);   // all lanes done reading the lists
+        grp.sync();   // every thread is done reading the lists
         // ---- apply the hop ----
         const bool fa = from < N, tb = to < N;
         for (int j = g; j < N; j += G) {
             float Ej = sm.E[j];
-            if (fa && j != from) Ej -= __ldg(&tab[j * S + from]).y;
-            if (tb && j != to) Ej += __ldg(&tab[j * S + to]).y;
+            if (fa && j != from) Ej -= pairs.coulomb(j, from);
+            if (tb && j != to) Ej += pairs.coulomb(j, to);
             sm.E[j] = Ej;
         }
         if (g == 0) {
@@ -356,7 +607,7 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
         }
         h += (tb ? 1 : 0) - (fa ? 1 : 0);
         ++hop;
-        __syncwarp(gmask);
+        grp.sync();
     }
 
     // ---- write back ----
@@ -373,34 +624,114 @@ __global__ void __launch_bounds__(256) f32_engine_kernel(const kmc_batch B)
         B.time[c] = t;
         B.hops_done[c] = hop;
         B.status[c] = status;
-        if (B.n_pairs) B.n_pairs[c] += pairs;
+        if (B.n_pairs) B.n_pairs[c] += npairs;
     }
 }
 
-template <int G>
-int launch(const kmc_batch &b, cudaStream_t st)
+// Warp-sliced kernel: 32/G chains per warp, warps_per_block warps.
+template <int G, typename Pairs>
+__global__ void __launch_bounds__(256) warp_engine_kernel(const kmc_batch B)
 {
     constexpr int CPW = 32 / G;
-    const int wpb = b.warps_per_block;
-    const size_t smem = static_cast<size_t>(wpb) * CPW * chain_smem_words(b.max_sites) * 4;
-    if (smem > 227 * 1024) return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds 227 KB", smem, b.max_sites, G, wpb);
-    // Raise the dynamic shared-memory limit only when a launch needs more than
-    // any before it, so launches under stream capture make no attribute calls
-    // once a first launch has run.
-    static int configured = 0;
-    cudaError_t e;
+    extern __shared__ __align__(16) uint32_t smem[];
+    WarpGroup<G> grp;
+    grp.init();
+    const int warp = threadIdx.x >> 5;
+    const int item = blockIdx.x * B.warps_per_block + warp;
+    if (item >= B.n_work) return;
+    const int c = B.work[item * CPW + grp.sub];
+    if (c < 0 || c >= B.n_chains) return;   // the whole group leaves together
+    using Rec = typename Pairs::Rec;
+    ChainSmem<Rec> sm = carve<Rec>(smem + (warp * CPW + grp.sub) * chain_smem_words<Rec>(B.max_sites),
+                                   B.max_sites);
+    run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c);
+}
+
+// Block kernel: one chain per block of T threads.
+template <int T, typename Pairs>
+__global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ double scratch[T / 32 + 2];
+    __shared__ int iscratch[2];
+    BlockGroup<T> grp;
+    grp.init();
+    grp.sd = scratch;
+    grp.si = iscratch;
+    const int c = B.work[blockIdx.x];
+    if (c < 0 || c >= B.n_chains) return;   // uniform over the block
+    using Rec = typename Pairs::Rec;
+    ChainSmem<Rec> sm = carve<Rec>(smem, B.max_sites);
+    run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c);
+}
+
+template <typename K>
+int set_smem(K kernel, size_t smem, int &configured)
+{
+    // Raise the dynamic shared-memory limit only when a launch needs more
+    // than any before it, so launches under stream capture make no
+    // attribute calls once a first launch has run.
     if (static_cast<int>(smem) > configured) {
-        e = cudaFuncSetAttribute(f32_engine_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem));
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
         if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(engine)");
         configured = static_cast<int>(smem);
     }
+    return KMC_OK;
+}
+
+template <int G, typename Pairs>
+int launch_warp(const kmc_batch &b, cudaStream_t st)
+{
+    constexpr int CPW = 32 / G;
+    const int wpb = b.warps_per_block;
+    const size_t smem = static_cast<size_t>(wpb) * CPW *
+                        chain_smem_words<typename Pairs::Rec>(b.max_sites) * 4;
+    if (smem > 227 * 1024)
+        return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds 227 KB",
+                    smem, b.max_sites, G, wpb);
+    static int configured = 0;
+    const int rc = set_smem(warp_engine_kernel<G, Pairs>, smem, configured);
+    if (rc != KMC_OK) return rc;
     const int grid = (b.n_work + wpb - 1) / wpb;
     if (grid <= 0) return KMC_OK;
-    f32_engine_kernel<G><<<grid, wpb * 32, smem, st>>>(b);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail_cuda(e, "engine launch");
-    return KMC_OK;
+    warp_engine_kernel<G, Pairs><<<grid, wpb * 32, smem, st>>>(b);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
+}
+
+template <int T, typename Pairs>
+int launch_block(const kmc_batch &b, cudaStream_t st)
+{
+    const size_t smem = static_cast<size_t>(chain_smem_words<typename Pairs::Rec>(b.max_sites)) * 4;
+    if (smem > 200 * 1024)
+        return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per chain (max_sites %d) exceeds the block budget",
+                    smem, b.max_sites);
+    static int configured = 0;
+    const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
+    if (rc != KMC_OK) return rc;
+    if (b.n_work <= 0) return KMC_OK;
+    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
+}
+
+template <typename Pairs>
+int dispatch(const kmc_batch &b, cudaStream_t st)
+{
+    switch (b.lanes_per_chain) {
+    case 4: return launch_warp<4, Pairs>(b, st);
+    case 8: return launch_warp<8, Pairs>(b, st);
+    case 16: return launch_warp<16, Pairs>(b, st);
+    case 32: return launch_warp<32, Pairs>(b, st);
+    case 64: return launch_block<64, Pairs>(b, st);
+    case 128: return launch_block<128, Pairs>(b, st);
+    case 256: return launch_block<256, Pairs>(b, st);
+    case 512: return launch_block<512, Pairs>(b, st);
+    default:
+        return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d not in {4,8,16,32,64,128,256,512}",
+                    b.lanes_per_chain);
+    }
 }
 
 }  // namespace
@@ -410,28 +741,29 @@ int run_batch(const kmc_batch &b, cudaStream_t st)
     if (b.n_chains < 0 || b.n_work < 0 || b.max_sites <= 0 || b.max_sites > kMaxSitesF32)
         return fail(KMC_ERR_INVALID, "engine: bad sizes (n_chains %d, n_work %d, max_sites %d)",
                     b.n_chains, b.n_work, b.max_sites);
-    if (b.warps_per_block < 1 || b.warps_per_block > 8)
+    if (b.lanes_per_chain <= 32 && (b.warps_per_block < 1 || b.warps_per_block > 8))
         return fail(KMC_ERR_INVALID, "engine: warps_per_block %d not in 1..8", b.warps_per_block);
     if (b.max_hops_per_launch <= 0)
         return fail(KMC_ERR_INVALID, "engine: max_hops_per_launch must be positive");
     if (b.record < 0 || b.record > 2) return fail(KMC_ERR_INVALID, "engine: bad record mode %d", b.record);
     if (b.record && (!b.occ_time || !b.occ_since || !b.traffic || !b.chain_pair_off))
         return fail(KMC_ERR_INVALID, "engine: record needs occ_time, occ_since, traffic, chain_pair_off");
-    if (!b.tab_N || !b.tab_P || !b.tab_off || !b.tab_LB || !b.chain_tab || !b.chain_kT ||
-        !b.chain_site_off || !b.chain_el_off || !b.E_constant || !b.el_energy || !b.occupation ||
+    if (!b.tab_N || !b.tab_P || !b.chain_tab || !b.chain_kT || !b.chain_site_off ||
+        !b.chain_el_off || !b.E_constant || !b.el_energy || !b.occupation ||
         !b.electrode_occupation || !b.time || !b.hops_done || !b.hops_total || !b.stream ||
         !b.status || !b.work)
         return fail(KMC_ERR_INVALID, "engine: a required pointer is NULL");
     if (b.replay && !b.replay_off) return fail(KMC_ERR_INVALID, "engine: replay needs replay_off");
-    switch (b.lanes_per_chain) {
-    case 4: return launch<4>(b, st);
-    case 8: return launch<8>(b, st);
-    case 16: return launch<16>(b, st);
-    case 32: return launch<32>(b, st);
-    default: return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d not in {4,8,16,32}", b.lanes_per_chain);
+    if (b.pair_mode == KMC_PAIRS_TABLE) {
+        if (!b.tab_off || !b.tab_LB) return fail(KMC_ERR_INVALID, "engine: table mode needs tab_off and tab_LB");
+        return dispatch<TablePairs>(b, st);
     }
+    if (b.pair_mode == KMC_PAIRS_POSITIONS) {
+        if (!b.tab_pos || !b.tab_pos_off || !b.tab_coef)
+            return fail(KMC_ERR_INVALID, "engine: positions mode needs tab_pos, tab_pos_off and tab_coef");
+        return dispatch<PositionPairs>(b, st);
+    }
+    return fail(KMC_ERR_INVALID, "engine: bad pair_mode %d", b.pair_mode);
 }
-
-int engine_smem_words(int max_sites) { return chain_smem_words(max_sites); }
 
 }  // namespace kmc

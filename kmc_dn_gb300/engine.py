@@ -27,7 +27,7 @@ import torch
 from . import _native
 from ._native import check, lib
 
-__all__ = ["simulate_f64", "TableSpec", "Batch", "simulate_cuda", "simulate_go", "superpose",
+__all__ = ["simulate_f64", "TableSpec", "TableSet", "Batch", "simulate_cuda", "simulate_go", "superpose",
            "default_lanes", "make_work_lists", "device", "prune"]
 
 
@@ -106,7 +106,14 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
 
 @dataclass
 class TableSpec:
-    """One geometry instance: the FP64 tables the hop loop reads."""
+    """One geometry instance: the FP64 tables the hop loop reads.
+
+    ``positions`` (S, 3: acceptors then electrodes) and ``ab`` are needed for
+    the positions pair mode, where the engine evaluates d_ij from the
+    coordinates; that mode is only valid when ``distances`` and
+    ``transitions_constant`` are the tables of those positions
+    (calc_distances / calc_transitions_constant), which ``check_positions``
+    verifies."""
     N: int
     P: int
     nu: float
@@ -114,22 +121,46 @@ class TableSpec:
     R: float
     distances: np.ndarray
     transitions_constant: np.ndarray
+    positions: Optional[np.ndarray] = None
+    ab: Optional[float] = None
 
     @property
     def S(self):
         return self.N + self.P
 
+    @classmethod
+    def from_network(cls, net):
+        pos = np.concatenate([np.asarray(net.acceptors, np.float64).reshape(-1, 3),
+                              np.asarray(net.electrodes, np.float64)[:, :3]], axis=0)
+        return cls(net.N, net.P, float(net.nu), float(net.I_0), float(net.R), net.distances,
+                   net.transitions_constant, pos, float(net.ab))
+
+    def check_positions(self, rtol=1e-9):
+        """True when the tables are those of the positions."""
+        if self.positions is None or self.ab is None:
+            return False
+        from . import geometry as geo
+        d = geo.site_distances(self.positions[: self.N], np.concatenate(
+            [self.positions[self.N:], np.zeros((self.P, 1))], axis=1))
+        tc = geo.transitions_constant(d, self.nu, self.ab)
+        return bool(np.allclose(d, self.distances, rtol=rtol, atol=0) and
+                    np.allclose(tc, self.transitions_constant, rtol=rtol, atol=1e-300))
+
 
 def default_lanes(S):
-    """Lanes per chain by size (the autotuner refines this per workload)."""
+    """Threads per chain by size (the autotuner refines this per workload):
+    warp slices for small networks, whole blocks for large ones."""
     if S <= 48:
-        return 8
-    if S <= 96:
         return 16
-    return 32
+    if S <= 128:
+        return 32
+    if S <= 512:
+        return 128
+    return 256
 
 
 _REANCHOR = 1024
+LANE_CHOICES = (4, 8, 16, 32, 64, 128, 256, 512)
 
 
 def make_work_lists(S_c, hops, lanes=None):
@@ -147,14 +178,14 @@ def make_work_lists(S_c, hops, lanes=None):
         lane_of = np.array([int(lanes(int(s))) for s in S_c], np.int32)
     else:
         lane_of = np.full(S_c.shape[0], int(lanes), np.int32)
-    bad = set(lane_of.tolist()) - {4, 8, 16, 32}
+    bad = set(lane_of.tolist()) - set(LANE_CHOICES)
     if bad:
-        raise ValueError(f"lanes per chain must be 4, 8, 16 or 32, got {sorted(bad)}")
+        raise ValueError(f"lanes per chain must be one of {LANE_CHOICES}, got {sorted(bad)}")
     out = []
     for G in sorted(set(lane_of.tolist())):
         idx = np.flatnonzero(lane_of == G)
         order = idx[np.lexsort((-hops[idx], -S_c[idx]))]
-        cpw = 32 // G
+        cpw = max(1, 32 // G)
         nw = (len(order) + cpw - 1) // cpw
         work = np.full(nw * cpw, -1, np.int32)
         work[: len(order)] = order
@@ -162,10 +193,61 @@ def make_work_lists(S_c, hops, lanes=None):
     return out
 
 
+class TableSet:
+    """Device-resident geometry data, built once and shared by batches:
+    FP32 pair tables (L, B) from the FP64 tables (kmc_build_table) and, in
+    positions mode, the site coordinates and rate constants."""
+
+    def __init__(self, specs: Sequence[TableSpec], pair_mode="table", dev=None):
+        d = device(dev)
+        self.specs = list(specs)
+        Ns = np.array([t.N for t in self.specs], np.int32)
+        Ps = np.array([t.P for t in self.specs], np.int32)
+        if np.any(Ps > 64):
+            raise ValueError("the engine supports at most 64 electrodes")
+        if pair_mode not in ("table", "positions"):
+            raise ValueError("pair_mode must be 'table' or 'positions'")
+        tab_off = np.zeros(len(self.specs), np.int64)
+        off = 0
+        for i, t in enumerate(self.specs):
+            tab_off[i] = off
+            off += 2 * t.S * t.S
+        self.tab_LB = torch.empty(max(off, 2), dtype=torch.float32, device=d)
+        L = lib()
+        sh = _stream_handle()
+        for i, t in enumerate(self.specs):
+            dd = _dev(np.asarray(t.distances, np.float64).reshape(t.S, t.S), torch.float64, d)
+            tc = _dev(np.asarray(t.transitions_constant, np.float64).reshape(t.S, t.S), torch.float64, d)
+            check(L.kmc_build_table(t.N, t.P, float(t.nu), float(t.I_0), float(t.R), _ptr(dd), _ptr(tc),
+                                    C.c_void_p(self.tab_LB.data_ptr() + 4 * int(tab_off[i])), sh))
+            torch.cuda.current_stream().synchronize()
+        self.tab_N = _dev(Ns, torch.int32, d)
+        self.tab_P = _dev(Ps, torch.int32, d)
+        self.tab_off = _dev(tab_off, torch.int64, d)
+        self.pair_mode = _native.PAIRS_POSITIONS if pair_mode == "positions" else _native.PAIRS_TABLE
+        self.tab_pos = self.tab_pos_off = self.tab_coef = None
+        if pair_mode == "positions":
+            pos_off = np.zeros(len(self.specs), np.int64)
+            rows, coef, off = [], [], 0
+            for i, t in enumerate(self.specs):
+                if not t.check_positions():
+                    raise ValueError(f"table {i}: positions mode needs tables computed from its positions")
+                p4 = np.zeros((t.S, 4), np.float32)
+                p4[:, :3] = t.positions
+                rows.append(p4.reshape(-1))
+                pos_off[i] = off
+                off += 4 * t.S
+                coef.append([-2.0 * np.log2(np.e) / t.ab, np.log2(t.nu * t.nu), t.I_0 * t.R, 0.0])
+            self.tab_pos = _dev(np.concatenate(rows), torch.float32, d)
+            self.tab_pos_off = _dev(pos_off, torch.int64, d)
+            self.tab_coef = _dev(np.asarray(coef, np.float32).reshape(-1), torch.float32, d)
+
+
 class Batch:
     """Device-resident chains for the batched FP32 engine.
 
-    tables:      list of TableSpec; chains name one by index.
+    tables:      list of TableSpec (or a prebuilt TableSet); chains name one
+                 by index.
     chain_table: (C,) table index per chain.
     kT:          (C,) temperature per chain.
     E_constant:  list of (N_c,) arrays, or a (C, N) array when all chains
@@ -180,13 +262,15 @@ class Batch:
                  S -> lanes.
     """
 
-    def __init__(self, tables: Sequence[TableSpec], chain_table, kT, E_constant=None,
+    def __init__(self, tables, chain_table, kT, E_constant=None,
                  el_energy=None, occupation=None, hops=None, *, streams=None, seed=0,
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
-                 replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR):
+                 replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
+                 pair_mode="table"):
         self.dev = device(dev)
         d = self.dev
-        self.tables = list(tables)
+        tables_set = tables if isinstance(tables, TableSet) else None
+        self.tables = list(tables.specs) if tables_set is not None else list(tables)
         ct = np.asarray(chain_table, np.int32).reshape(-1)
         self.n = n = ct.shape[0]
         self.chain_table = ct
@@ -202,24 +286,11 @@ class Batch:
         self.reanchor = int(reanchor)
         self.warps_per_block = int(warps_per_block)
 
-        # tables -> FP32 (L, B) on device
-        tab_off = np.zeros(len(self.tables), np.int64)
-        off = 0
-        for i, t in enumerate(self.tables):
-            tab_off[i] = off
-            off += 2 * t.S * t.S
-        self.tab_LB = torch.empty(max(off, 2), dtype=torch.float32, device=d)
-        L = lib()
-        sh = _stream_handle()
-        for i, t in enumerate(self.tables):
-            dd = _dev(np.asarray(t.distances, np.float64).reshape(t.S, t.S), torch.float64, d)
-            tc = _dev(np.asarray(t.transitions_constant, np.float64).reshape(t.S, t.S), torch.float64, d)
-            check(L.kmc_build_table(t.N, t.P, float(t.nu), float(t.I_0), float(t.R), _ptr(dd), _ptr(tc),
-                                    C.c_void_p(self.tab_LB.data_ptr() + 4 * int(tab_off[i])), sh))
-            torch.cuda.current_stream().synchronize()
-        self.tab_N = _dev(Ns, torch.int32, d)
-        self.tab_P = _dev(Ps, torch.int32, d)
-        self.tab_off = _dev(tab_off, torch.int64, d)
+        ts = tables_set if tables_set is not None else TableSet(self.tables, pair_mode=pair_mode, dev=d)
+        self.table_set = ts
+        self.tab_N, self.tab_P, self.tab_off, self.tab_LB = ts.tab_N, ts.tab_P, ts.tab_off, ts.tab_LB
+        self.pair_mode = ts.pair_mode
+        self.tab_pos, self.tab_pos_off, self.tab_coef = ts.tab_pos, ts.tab_pos_off, ts.tab_coef
 
         # per-chain offsets
         self.site_off = np.concatenate([[0], np.cumsum(self.N_c)[:-1]]).astype(np.int64)
@@ -276,7 +347,7 @@ class Batch:
     def _make_bins(self, lanes, hops):
         bins = []
         for G, work, order, smax in make_work_lists(self.S_c, hops, lanes):
-            bins.append(dict(G=G, n_work=len(work) // (32 // G), work=_dev(work, torch.int32, self.dev),
+            bins.append(dict(G=G, n_work=len(work) // max(1, 32 // G), work=_dev(work, torch.int32, self.dev),
                              max_sites=smax, chains=order))
         return bins
 
@@ -317,6 +388,10 @@ class Batch:
             b.replay, b.replay_off = self.replay.data_ptr(), self.replay_off.data_ptr()
         if self.cancel is not None:
             b.cancel = self.cancel
+        b.pair_mode = self.pair_mode
+        if self.tab_pos is not None:
+            b.tab_pos, b.tab_pos_off, b.tab_coef = (self.tab_pos.data_ptr(), self.tab_pos_off.data_ptr(),
+                                                    self.tab_coef.data_ptr())
         return b
 
     def launch(self, max_hops_per_launch=None, stream=None):

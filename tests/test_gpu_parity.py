@@ -68,21 +68,24 @@ def test_f64_philox_mode_runs(engine_lib):
     assert np.any(a["hop_log"] != c["hop_log"])
 
 
-def _batch_one(g, hops, uniforms=None, record=0, lanes=8, seed=0):
+def _batch_one(g, hops, uniforms=None, record=0, lanes=8, seed=0, pair_mode="table", spec=None):
     from kmc_dn_gb300.engine import Batch, TableSpec
     N, P = int(g["N"]), int(g["P"])
-    spec = TableSpec(N, P, float(g["nu"]), float(g["I_0"]), float(g["R"]), g["distances"],
-                     g["transitions_constant"])
+    if spec is None:
+        spec = TableSpec(N, P, float(g["nu"]), float(g["I_0"]), float(g["R"]), g["distances"],
+                         g["transitions_constant"])
     se = np.asarray(g["site_energies"], np.float64)
     b = Batch([spec], [0], [float(g["kT"])], [g["E_constant"]], [se[N:]], [g["occupation"]], [hops],
               seed=seed, record=record, lanes=lanes,
-              replay=[uniforms] if uniforms is not None else None)
+              replay=[uniforms] if uniforms is not None else None, pair_mode=pair_mode)
     b.run()
     return b.results()
 
 
-@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
-def test_f32_engine_replay_agrees_where_margins_allow(engine_lib, oracle_mod, lanes):
+@pytest.mark.parametrize("lanes,pair_mode", [(4, "table"), (8, "table"), (16, "table"), (32, "table"),
+                                              (64, "table"), (128, "table"), (16, "positions"),
+                                              (32, "positions"), (128, "positions")])
+def test_f32_engine_replay_agrees_where_margins_allow(engine_lib, oracle_mod, lanes, pair_mode):
     """Fed the same stream, the FP32 engine picks the reference's pair on every
     hop whose event uniform is further than 1e-4 (relative) from a cumulative
     boundary; the sequences may part only after the first closer call."""
@@ -96,7 +99,13 @@ def test_f32_engine_replay_agrees_where_margins_allow(engine_lib, oracle_mod, la
     close = np.flatnonzero(o["margins"] < 1e-4)
     safe = int(close[0]) if close.size else hops
     assert safe > 50
-    r = _batch_one(g, safe, uniforms=u, record=1, lanes=lanes)
+    spec = None
+    if pair_mode == "positions":
+        from kmc_dn_gb300 import workloads
+        from kmc_dn_gb300.engine import TableSpec
+        spec = TableSpec.from_network(workloads.plain_network(0))   # the golden's network
+        np.testing.assert_array_equal(spec.distances, g["distances"])
+    r = _batch_one(g, safe, uniforms=u, record=1, lanes=lanes, pair_mode=pair_mode, spec=spec)
     assert r["status"][0] == 0
     # the final state after `safe` hops equals the oracle's state after `safe` hops
     o2 = oracle_mod.numba_replay(int(g["N"]), int(g["P"]), float(g["nu"]), float(g["kT"]),
@@ -229,3 +238,45 @@ def test_no_allowed_transition_reports_status(engine_lib):
     assert r["status"] == KMC_ERR_NONFINITE
     b = Batch([TableSpec(1, 0, 1.0, 1.0, 1.0, d, tc)], [0], [1.0], [[0.0]], [[]], [[1]], [10], lanes=4)
     assert b.run().results()["status"][0] == KMC_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("lanes,pair_mode", [(32, "table"), (128, "table"), (128, "positions"),
+                                              (256, "positions")])
+def test_f32_engine_large_network_replay(engine_lib, oracle_mod, lanes, pair_mode):
+    """A 300-acceptor network (block groups, multi-word occupancy bitmask):
+    the engine follows the FP64 oracle over the hops whose margins allow."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import TableSpec
+    net = workloads.large_network(seed=3, N=300, M=30)
+    hops = 400
+    u = replay_uniforms(41, 2 * hops)
+    occ = net.occupation.astype(np.uint8)
+    o = oracle_mod.numba_replay(net.N, net.P, net.nu, net.kT, net.I_0, net.R, occ, net.distances,
+                                net.E_constant(), net.site_energies(), net.transitions_constant, u,
+                                hops=hops, record=False)
+    close = np.flatnonzero(o["margins"] < 1e-4)
+    safe = int(close[0]) if close.size else hops
+    assert safe >= 20
+    o2 = oracle_mod.numba_replay(net.N, net.P, net.nu, net.kT, net.I_0, net.R, occ, net.distances,
+                                 net.E_constant(), net.site_energies(), net.transitions_constant, u,
+                                 hops=safe, record=False)
+    g = dict(N=net.N, P=net.P, nu=net.nu, kT=net.kT, I_0=net.I_0, R=net.R, occupation=occ,
+             distances=net.distances, E_constant=net.E_constant(), site_energies=net.site_energies(),
+             transitions_constant=net.transitions_constant)
+    r = _batch_one(g, safe, uniforms=u, lanes=lanes, pair_mode=pair_mode,
+                   spec=TableSpec.from_network(net))
+    assert r["status"][0] == 0
+    np.testing.assert_array_equal(r["occupation"][0], o2["occupation"].astype(bool))
+    np.testing.assert_array_equal(r["electrode_occupation"][0], o2["electrode_occupation"])
+    assert abs(r["time"][0] - o2["time"]) <= 1e-4 * o2["time"]
+
+
+def test_positions_mode_rejects_inconsistent_tables(engine_lib):
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    net = workloads.plain_network(0)
+    spec = TableSpec.from_network(net)
+    spec.transitions_constant = spec.transitions_constant * 1.5     # e.g. ab changed, tc not recomputed
+    with pytest.raises(ValueError):
+        Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]],
+              [net.occupation.astype(np.uint8)], [10], pair_mode="positions")

@@ -12,7 +12,7 @@ def test_work_lists_cover_every_chain_once():
     hops = rng.integers(1, 10**6, 1000)
     seen = []
     for G, work, order, smax in make_work_lists(S, hops):
-        assert len(work) % (32 // G) == 0
+        assert len(work) % max(1, 32 // G) == 0
         ids = work[work >= 0]
         assert np.all([default_lanes(int(S[i])) == G for i in ids])
         assert smax == S[ids].max()
