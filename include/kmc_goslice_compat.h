@@ -65,6 +65,14 @@ int64_t parallelSimulations(GoSlice NSites, GoSlice NElectrodes, GoSlice nu, GoS
                             GoSlice electrode_occupation, GoSlice hops, GoSlice time,
                             GoSlice site_energies);
 
+/* Returns sum_k (k+1) * s_k.len over fourteen slices, touching nothing else:
+ * lets a caller check that its FFI passes fourteen GoSlice arguments the way
+ * the platform's C ABI does before it calls parallelSimulations.  No
+ * reference counterpart (diagnostic). */
+int64_t kmc_goslice_abi_probe(GoSlice s0, GoSlice s1, GoSlice s2, GoSlice s3, GoSlice s4,
+                              GoSlice s5, GoSlice s6, GoSlice s7, GoSlice s8, GoSlice s9,
+                              GoSlice s10, GoSlice s11, GoSlice s12, GoSlice s13);
+
 #ifdef __cplusplus
 }
 #endif

@@ -324,6 +324,7 @@ struct BlockGroup {
 // Per-chain shared memory
 // ---------------------------------------------------------------------------
 
+
 template <typename Rec>
 struct ChainSmem {
     Rec *src;        // [S+1] source records
@@ -333,10 +334,11 @@ struct ChainSmem {
     float *E;        // [S]   site energies (acceptors)
     uint32_t *occw;  // [W]   occupancy bits
     int *eo;         // [kMaxElectrodes] electrode counters of this launch
+    float *rates;    // [rate_words] this hop's pair rates, or nullptr (recompute)
 };
 
 template <typename Rec>
-__host__ __device__ __forceinline__ int chain_smem_words(int S)
+__host__ __device__ __forceinline__ int chain_list_words(int S)
 {
     const int W = (S + 31) / 32;
     const int rw = static_cast<int>(sizeof(Rec) / 4);
@@ -344,8 +346,16 @@ __host__ __device__ __forceinline__ int chain_smem_words(int S)
     return (words + 3) & ~3;
 }
 
+// Words to keep every pair rate of one hop: A(h) <= S^2/3 for any split of
+// S sites into acceptors and electrodes, plus one row of G for the
+// transposed layout.
+__host__ __device__ __forceinline__ int rate_buffer_words(int S, int G)
+{
+    return (((S * S) / 3 + 1 + G) + 3) & ~3;
+}
+
 template <typename Rec>
-__device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S)
+__device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_words)
 {
     ChainSmem<Rec> c;
     c.src = reinterpret_cast<Rec *>(base);
@@ -355,6 +365,7 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S)
     c.E = reinterpret_cast<float *>(c.tgt_id + (S + 1));
     c.occw = reinterpret_cast<uint32_t *>(c.E + S);
     c.eo = reinterpret_cast<int *>(c.occw + (S + 31) / 32);
+    c.rates = rate_words > 0 ? reinterpret_cast<float *>(base + chain_list_words<Rec>(S)) : nullptr;
     return c;
 }
 
@@ -420,54 +431,56 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     if (record)
         for (int j = g; j < N; j += G) occ_since[j] = t;
 
+    // Energies from scratch (E_j = Ec_j - sum_{k empty} B_jk) and the ordered
+    // lists built from them.  Run at the launch start and at every absolute
+    // hop index that is a multiple of `reanchor`, so a run split into
+    // launches anchors at the same hops.
+    auto anchor_and_build = [&]() {
+        for (int j = g; j < N; j += G) {
+            float acc = 0.0f;
+            for (int k = 0; k < N; ++k)
+                if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += pairs.coulomb(j, k);
+            sm.E[j] = Ec[j] - acc;
+        }
+        const int z = N - h;
+        int wcur = 0, cum = 0;
+        for (int j = g; j < N; j += G) {
+            const int w = j >> 5;
+            while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
+            const uint32_t word = sm.occw[w];
+            const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
+            const Rec r = pairs.rec(j, cs * sm.E[j]);
+            if ((word >> (j & 31)) & 1u) { sm.src[below] = r; sm.src_id[below] = j; }
+            else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
+        }
+        for (int e = g; e < P; e += G) {
+            const Rec r = pairs.rec(N + e, cs * Vel[e]);
+            sm.src[h + e] = r;
+            sm.src_id[h + e] = N + e;
+            sm.tgt[z + e] = r;
+            sm.tgt_id[z + e] = N + e;
+        }
+        grp.sync();
+    };
+    anchor_and_build();
+    int until_anchor = reanchor - static_cast<int>(hop % reanchor);
+
     // Philox words: thread g holds the draw of hop rbase + (g mod 32)
     u32x4 rnd{0, 0, 0, 0};
     int64_t rbase = INT64_MIN / 2;
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
-    // hops until the next multiple of `reanchor` (anchors fall on absolute
-    // hop indices, so a run split into launches anchors at the same hops)
-    int until_anchor = 0;   // anchor at the launch start as well
-    const int phase0 = static_cast<int>(hop % reanchor);
 
     while (hop < hop_end) {
         if (B.cancel && (hop & 1023) == 0) {
             const int stop = grp.bcast(g == 0 ? *B.cancel : 0, 0);
             if (stop) { status = KMC_ERR_CANCELLED; break; }
         }
-        // ---- (re)anchor energies: E_j = Ec_j - sum_{k empty} B_jk ----
         if (until_anchor == 0) {
-            for (int j = g; j < N; j += G) {
-                float acc = 0.0f;
-                for (int k = 0; k < N; ++k)
-                    if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += pairs.coulomb(j, k);
-                sm.E[j] = Ec[j] - acc;
-            }
-            until_anchor = (hop == hops_done0 && phase0 != 0) ? reanchor - phase0 : reanchor;
-            grp.sync();
+            grp.sync();           // bit updates of the last hop are visible
+            anchor_and_build();
+            until_anchor = reanchor;
         }
         --until_anchor;
-        // ---- site phase: rebuild ordered source / target lists ----
-        {
-            const int z = N - h;
-            int wcur = 0, cum = 0;
-            for (int j = g; j < N; j += G) {
-                const int w = j >> 5;
-                while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
-                const uint32_t word = sm.occw[w];
-                const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
-                const Rec r = pairs.rec(j, cs * sm.E[j]);
-                if ((word >> (j & 31)) & 1u) { sm.src[below] = r; sm.src_id[below] = j; }
-                else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
-            }
-            for (int e = g; e < P; e += G) {
-                const Rec r = pairs.rec(N + e, cs * Vel[e]);
-                sm.src[h + e] = r;
-                sm.src_id[h + e] = N + e;
-                sm.tgt[z + e] = r;
-                sm.tgt_id[z + e] = N + e;
-            }
-            grp.sync();
-        }
         // ---- pair phase ----
         const int z = N - h;
         const int T1 = z + P, T2 = z;
@@ -479,44 +492,30 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const int M = (A + G - 1) / G;
         float lsum = 0.0f;
         {
-            // The thread's run is walked as U contiguous sub-runs in lock
-            // step: U independent load -> rate -> sum chains per iteration.
-            constexpr int U = 4;
+            // The thread walks its contiguous run of pairs row by row; rates
+            // are kept (transposed: element i of thread g at i*G + g) when
+            // the shared-memory budget allows, for the event search below.
             const int kb = g * M;
             const int ke = min(kb + M, A);
             if (kb < ke) {
-                const int m = (ke - kb + U - 1) / U;
-                int row[U], col[U], Tc[U], left[U];
-                bool sa[U];
-                Rec sr[U];
-                float acc[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int s0 = kb + u * m;
-                    left[u] = max(0, min(m, ke - s0));
-                    acc[u] = 0.0f;
-                    row[u] = col[u] = 0;
-                    if (left[u] > 0) decode_pair(s0, h, A1, T1, T2, inv1, inv2, row[u], col[u]);
-                    sa[u] = row[u] < h;
-                    Tc[u] = sa[u] ? T1 : T2;
-                    sr[u] = sm.src[row[u]];
-                }
-                for (int it = 0; it < m; ++it) {
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        if (it < left[u]) {
-                            acc[u] += pairs.rate(sr[u], sm.tgt[col[u]], sa[u] && col[u] < z, cs);
-                            if (++col[u] == Tc[u]) {
-                                col[u] = 0;
-                                ++row[u];
-                                sa[u] = row[u] < h;
-                                Tc[u] = sa[u] ? T1 : T2;
-                                sr[u] = sm.src[row[u]];
-                            }
-                        }
+                int row, col;
+                decode_pair(kb, h, A1, T1, T2, inv1, inv2, row, col);
+                bool sa = row < h;
+                int Tc = sa ? T1 : T2;
+                Rec sr = sm.src[row];
+                float *rp = sm.rates ? sm.rates + g : nullptr;
+                for (int k = kb; k < ke; ++k) {
+                    const float r = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                    lsum += r;
+                    if (rp) { *rp = r; rp += G; }
+                    if (++col == Tc) {
+                        col = 0;
+                        ++row;
+                        sa = row < h;
+                        Tc = sa ? T1 : T2;
+                        sr = sm.src[row];
                     }
                 }
-                lsum = ((acc[0] + acc[1]) + acc[2]) + acc[3];
             }
         }
         npairs += static_cast<unsigned long long>(A);
@@ -541,6 +540,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             e1 = -__logf(u01_from32(w0));
             u_ev = u01_from52(w1, w2);
         }
+        if (sm.rates) grp.sync();   // stored rates visible to the whole group
         // ---- FP64 scan of the per-thread sums ----
         double excl, tot;
         const double incl = grp.scan(static_cast<double>(lsum), excl, tot);
@@ -550,26 +550,31 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (L < 0) L = G - 1;
         const double baseL = grp.bcast(excl, L);
         float rem = static_cast<float>(target - baseL);
-        // ---- re-evaluate thread L's run and find the event ----
+        // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         {
             const int kb = L * M;
             const int ke = min(kb + M, A);
-            for (int kc = kb; kc < ke; kc += G) {
-                const int k = kc + g;
+            const int len = ke - kb;
+            for (int i0 = 0; i0 < len; i0 += G) {
+                const int i = i0 + g;
                 float r = 0.0f;
-                if (k < ke) {
-                    int row, col;
-                    decode_pair(k, h, A1, T1, T2, inv1, inv2, row, col);
-                    r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
+                if (i < len) {
+                    if (sm.rates) {
+                        r = sm.rates[i * G + L];   // pair kb + i, stored by thread L
+                    } else {
+                        int row, col;
+                        decode_pair(kb + i, h, A1, T1, T2, inv1, inv2, row, col);
+                        r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
+                    }
                 }
                 float ctot;
                 const float q = grp.scanf(r, ctot);
-                const bool pos = (k < ke) && (r > 0.0f);
+                const bool pos = (i < len) && (r > 0.0f);
                 const int hit = grp.first(pos && q >= rem);
-                if (hit >= 0) { chosen = kc + hit; break; }
+                if (hit >= 0) { chosen = kb + i0 + hit; break; }
                 const int lp = grp.last(pos);
-                if (lp >= 0) last_pos = kc + lp;
+                if (lp >= 0) last_pos = kb + i0 + lp;
                 rem -= ctot;
             }
         }
@@ -583,15 +588,40 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const float dt = e1 * __frcp_rn(static_cast<float>(tot));
         const double t_before = t;
         t += static_cast<double>(dt);
-        grp.sync();   // every thread is done reading the lists
-        // ---- apply the hop ----
+        grp.sync();   // every thread is done reading the lists and rates
+        // ---- apply the hop and rebuild the lists in one pass ----
         const bool fa = from < N, tb = to < N;
-        for (int j = g; j < N; j += G) {
-            float Ej = sm.E[j];
-            if (fa && j != from) Ej -= pairs.coulomb(j, from);
-            if (tb && j != to) Ej += pairs.coulomb(j, to);
-            sm.E[j] = Ej;
+        const int h_new = h + (tb ? 1 : 0) - (fa ? 1 : 0);
+        const int z_new = N - h_new;
+        {
+            int wcur = 0, cum = 0;
+            for (int j = g; j < N; j += G) {
+                float Ej = sm.E[j];
+                if (fa && j != from) Ej -= pairs.coulomb(j, from);
+                if (tb && j != to) Ej += pairs.coulomb(j, to);
+                sm.E[j] = Ej;
+                const int w = j >> 5;
+                while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
+                const uint32_t word = sm.occw[w];
+                // holes below j and the bit of j after the hop
+                const int below = cum + __popc(word & ((1u << (j & 31)) - 1u))
+                                  - ((fa && from < j) ? 1 : 0) + ((tb && to < j) ? 1 : 0);
+                const bool occ_j = (j == to && tb) || (j != from && ((word >> (j & 31)) & 1u));
+                const Rec r = pairs.rec(j, cs * Ej);
+                if (occ_j) { sm.src[below] = r; sm.src_id[below] = j; }
+                else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
+            }
+            if (h_new != h) {
+                for (int e = g; e < P; e += G) {
+                    const Rec r = pairs.rec(N + e, cs * Vel[e]);
+                    sm.src[h_new + e] = r;
+                    sm.src_id[h_new + e] = N + e;
+                    sm.tgt[z_new + e] = r;
+                    sm.tgt_id[z_new + e] = N + e;
+                }
+            }
         }
+        grp.sync();   // lists complete; the bitmask is read no more this hop
         if (g == 0) {
             if (fa) sm.occw[from >> 5] &= ~(1u << (from & 31));
             else sm.eo[from - N] -= 1;
@@ -605,10 +635,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 if (tb) occ_since[to] = tx;
             }
         }
-        h += (tb ? 1 : 0) - (fa ? 1 : 0);
+        h = h_new;
         ++hop;
-        grp.sync();
     }
+    grp.sync();
 
     // ---- write back ----
     if (record) {
@@ -628,9 +658,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     }
 }
 
-// Warp-sliced kernel: 32/G chains per warp, warps_per_block warps.
+// Warp-sliced kernel: 32/G chains per warp, warps_per_block warps.  The
+// bound of 3 blocks of 256 threads keeps registers at or below 85 so that
+// 24 warps fit on an SM.
 template <int G, typename Pairs>
-__global__ void __launch_bounds__(256) warp_engine_kernel(const kmc_batch B)
+__global__ void __launch_bounds__(256, 3) warp_engine_kernel(const kmc_batch B, int rate_words)
 {
     constexpr int CPW = 32 / G;
     extern __shared__ __align__(16) uint32_t smem[];
@@ -642,14 +674,14 @@ __global__ void __launch_bounds__(256) warp_engine_kernel(const kmc_batch B)
     const int c = B.work[item * CPW + grp.sub];
     if (c < 0 || c >= B.n_chains) return;   // the whole group leaves together
     using Rec = typename Pairs::Rec;
-    ChainSmem<Rec> sm = carve<Rec>(smem + (warp * CPW + grp.sub) * chain_smem_words<Rec>(B.max_sites),
-                                   B.max_sites);
+    const int words = chain_list_words<Rec>(B.max_sites) + rate_words;
+    ChainSmem<Rec> sm = carve<Rec>(smem + (warp * CPW + grp.sub) * words, B.max_sites, rate_words);
     run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c);
 }
 
 // Block kernel: one chain per block of T threads.
 template <int T, typename Pairs>
-__global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B)
+__global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B, int rate_words)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ double scratch[T / 32 + 2];
@@ -661,7 +693,7 @@ __global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B)
     const int c = B.work[blockIdx.x];
     if (c < 0 || c >= B.n_chains) return;   // uniform over the block
     using Rec = typename Pairs::Rec;
-    ChainSmem<Rec> sm = carve<Rec>(smem, B.max_sites);
+    ChainSmem<Rec> sm = carve<Rec>(smem, B.max_sites, rate_words);
     run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c);
 }
 
@@ -680,22 +712,26 @@ int set_smem(K kernel, size_t smem, int &configured)
     return KMC_OK;
 }
 
+constexpr size_t kSmemBudget = 200 * 1024;   // per block, leaving room for static scratch
+
 template <int G, typename Pairs>
 int launch_warp(const kmc_batch &b, cudaStream_t st)
 {
     constexpr int CPW = 32 / G;
     const int wpb = b.warps_per_block;
-    const size_t smem = static_cast<size_t>(wpb) * CPW *
-                        chain_smem_words<typename Pairs::Rec>(b.max_sites) * 4;
-    if (smem > 227 * 1024)
-        return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds 227 KB",
+    const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
+    int rw = rate_buffer_words(b.max_sites, G);
+    if (static_cast<size_t>(wpb) * CPW * (lw + rw) * 4 > kSmemBudget) rw = 0;   // recompute instead
+    const size_t smem = static_cast<size_t>(wpb) * CPW * (lw + rw) * 4;
+    if (smem > kSmemBudget)
+        return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds the budget",
                     smem, b.max_sites, G, wpb);
     static int configured = 0;
     const int rc = set_smem(warp_engine_kernel<G, Pairs>, smem, configured);
     if (rc != KMC_OK) return rc;
     const int grid = (b.n_work + wpb - 1) / wpb;
     if (grid <= 0) return KMC_OK;
-    warp_engine_kernel<G, Pairs><<<grid, wpb * 32, smem, st>>>(b);
+    warp_engine_kernel<G, Pairs><<<grid, wpb * 32, smem, st>>>(b, rw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }
@@ -703,15 +739,18 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
 template <int T, typename Pairs>
 int launch_block(const kmc_batch &b, cudaStream_t st)
 {
-    const size_t smem = static_cast<size_t>(chain_smem_words<typename Pairs::Rec>(b.max_sites)) * 4;
-    if (smem > 200 * 1024)
+    const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
+    int rw = rate_buffer_words(b.max_sites, T);
+    if (static_cast<size_t>(lw + rw) * 4 > kSmemBudget) rw = 0;
+    const size_t smem = static_cast<size_t>(lw + rw) * 4;
+    if (smem > kSmemBudget)
         return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per chain (max_sites %d) exceeds the block budget",
                     smem, b.max_sites);
     static int configured = 0;
     const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
     if (rc != KMC_OK) return rc;
     if (b.n_work <= 0) return KMC_OK;
-    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b);
+    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }

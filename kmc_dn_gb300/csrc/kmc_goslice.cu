@@ -200,4 +200,14 @@ int64_t parallelSimulations(GoSlice NSites, GoSlice NElectrodes, GoSlice nu, GoS
     return 0;
 }
 
+int64_t kmc_goslice_abi_probe(GoSlice s0, GoSlice s1, GoSlice s2, GoSlice s3, GoSlice s4,
+                              GoSlice s5, GoSlice s6, GoSlice s7, GoSlice s8, GoSlice s9,
+                              GoSlice s10, GoSlice s11, GoSlice s12, GoSlice s13)
+{
+    const GoSlice s[14] = {s0, s1, s2, s3, s4, s5, s6, s7, s8, s9, s10, s11, s12, s13};
+    int64_t acc = 0;
+    for (int k = 0; k < 14; ++k) acc += (k + 1) * s[k].len;
+    return acc;
+}
+
 }  // extern "C"

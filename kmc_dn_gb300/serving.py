@@ -83,7 +83,8 @@ class Server:
                  pair_mode="positions", lanes=None, dev=None, short_hops=20000):
         if quantum % _REANCHOR:
             raise ValueError("quantum must be a multiple of the re-anchor period (1024)")
-        self.dev = torch.device(dev if dev is not None else "cuda")
+        d = torch.device(dev if dev is not None else "cuda")
+        self.dev = torch.device("cuda", d.index if d.index is not None else torch.cuda.current_device())
         self.networks = list(networks)
         self.quantum = int(quantum)
         self.pair_mode = pair_mode

@@ -90,12 +90,30 @@ class Network:
         return se
 
 
+_UNIT_BASIS = {}
+
+
+def unit_square_basis(electrodes_unit, cells):
+    """Basis fields of a square with electrodes at the given positions in
+    unit coordinates.  The Laplace problem is scale invariant and the
+    electrode segment half-width (xdim/10) scales with the side, so every
+    square network with the same relative electrode layout shares them."""
+    key = (tuple(map(tuple, np.round(np.asarray(electrodes_unit, np.float64), 12))), int(cells))
+    bf = _UNIT_BASIS.get(key)
+    if bf is None:
+        bf = solve_basis_fields(1.0, 1.0, np.asarray(electrodes_unit, np.float64), cells, cells)
+        _UNIT_BASIS[key] = bf
+    return bf
+
+
 def make_network(rng, N, M, xdim, ydim, electrodes_xy, *, voltages, I_0=50.0, a=1.0,
                  kT=1.0, nu=1.0, mu=0.0, cells=100, ab_over_R=None):
     """Build a 2D network with random acceptors/donors and the given electrodes.
 
     I_0 is in units of kT as in the constructor (``I_0 = I_0_arg * kT``,
-    kmc_dopant_networks.py:338); ab = a*R (:361) unless ab_over_R is given."""
+    kmc_dopant_networks.py:338); ab = a*R (:361) unless ab_over_R is given.
+    Square domains reuse the unit-square basis fields of their electrode
+    layout."""
     R, dim = geo.dimensionless_R(N, xdim, ydim, 0)
     assert dim == 2
     acc, don = geo.place_dopants(rng, N, M, xdim, ydim, 0)
@@ -109,8 +127,12 @@ def make_network(rng, N, M, xdim, ydim, electrodes_xy, *, voltages, I_0=50.0, a=
     dist = geo.site_distances(acc, el)
     tc = geo.transitions_constant(dist, nu, ab)
     comp = geo.compensation(acc, don, I0, R)
-    bf = solve_basis_fields(xdim, ydim, el[:, :2], cells, cells)
-    basis = bf.sample(acc[:, :2])
+    if xdim == ydim:
+        bf = unit_square_basis(el[:, :2] / xdim, cells)
+        basis = bf.sample(acc[:, :2] / xdim)
+    else:
+        bf = solve_basis_fields(xdim, ydim, el[:, :2], cells, cells)
+        basis = bf.sample(acc[:, :2])
     return Network(N=N, M=M, xdim=float(xdim), ydim=float(ydim), zdim=0.0, acceptors=acc,
                    donors=don, electrodes=el, nu=float(nu), kT=float(kT), I_0=float(I0),
                    R=float(R), ab=float(ab), mu=float(mu), distances=dist,

@@ -249,7 +249,7 @@ def test_f32_engine_large_network_replay(engine_lib, oracle_mod, lanes, pair_mod
     from kmc_dn_gb300.engine import TableSpec
     net = workloads.large_network(seed=3, N=300, M=30)
     hops = 400
-    u = replay_uniforms(41, 2 * hops)
+    u = replay_uniforms(50, 2 * hops)
     occ = net.occupation.astype(np.uint8)
     o = oracle_mod.numba_replay(net.N, net.P, net.nu, net.kT, net.I_0, net.R, occ, net.distances,
                                 net.E_constant(), net.site_energies(), net.transitions_constant, u,
