@@ -492,9 +492,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const int M = (A + G - 1) / G;
         float lsum = 0.0f;
         {
-            // The thread walks its contiguous run of pairs row by row; rates
-            // are kept (transposed: element i of thread g at i*G + g) when
-            // the shared-memory budget allows, for the event search below.
+            // The thread walks its contiguous run of pairs in row-major order,
+            // two pairs per step (two independent load -> rate chains; a row
+            // change is a select, not a branch).  When the shared-memory
+            // budget allows, the running sum after every pair is kept
+            // (transposed: element i of thread g at i*G + g) for the event
+            // search below.
             const int kb = g * M;
             const int ke = min(kb + M, A);
             if (kb < ke) {
@@ -504,17 +507,34 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 int Tc = sa ? T1 : T2;
                 Rec sr = sm.src[row];
                 float *rp = sm.rates ? sm.rates + g : nullptr;
-                for (int k = kb; k < ke; ++k) {
-                    const float r = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    lsum += r;
-                    if (rp) { *rp = r; rp += G; }
-                    if (++col == Tc) {
-                        col = 0;
-                        ++row;
-                        sa = row < h;
-                        Tc = sa ? T1 : T2;
-                        sr = sm.src[row];
-                    }
+                int k = kb;
+                for (; k + 1 < ke; k += 2) {
+                    // second pair of the step
+                    const bool wa = (col + 1 == Tc);
+                    const int colb = wa ? 0 : col + 1;
+                    const int rowb = row + (wa ? 1 : 0);
+                    const Rec srn = sm.src[rowb];
+                    const Rec srb = wa ? srn : sr;
+                    const bool sab = rowb < h;
+                    const int Tcb = sab ? T1 : T2;
+                    const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                    const float rb = pairs.rate(srb, sm.tgt[colb], sab && colb < z, cs);
+                    lsum += ra;
+                    if (rp) { rp[0] = lsum; }
+                    lsum += rb;
+                    if (rp) { rp[G] = lsum; rp += 2 * G; }
+                    // advance past the second pair
+                    const bool wb = (colb + 1 == Tcb);
+                    col = wb ? 0 : colb + 1;
+                    row = rowb + (wb ? 1 : 0);
+                    const Rec srm = sm.src[row];
+                    sr = wb ? srm : srb;
+                    sa = row < h;
+                    Tc = sa ? T1 : T2;
+                }
+                if (k < ke) {
+                    lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                    if (rp) rp[0] = lsum;
                 }
             }
         }
@@ -552,7 +572,30 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         float rem = static_cast<float>(target - baseL);
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
-        {
+        if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
+        if (sm.rates) {
+            // Thread L kept its running sums: the event is the first pair whose
+            // sum reaches rem.  Each thread of the group searches one block of
+            // them; the lowest block with a hit wins.
+            const int len = min(M, A - L * M);
+            const int Bk = (len + G - 1) / G;
+            const int i0 = g * Bk, i1 = min(i0 + Bk, len);
+            int found = -1;
+            for (int i = i0; i < i1; ++i)
+                if (sm.rates[i * G + L] >= rem) { found = i; break; }
+            const int hl = grp.first(found >= 0);
+            if (hl >= 0) {
+                chosen = L * M + grp.bcast(found, hl);
+            } else if (len > 0) {
+                // rem rounded above the run's total: the run's last pair
+                // with a positive rate
+                int lp = -1;
+                for (int i = i0; i < i1; ++i)
+                    if (sm.rates[i * G + L] > (i > 0 ? sm.rates[(i - 1) * G + L] : 0.0f)) lp = i;
+                const int ll = grp.last(lp >= 0);
+                if (ll >= 0) chosen = L * M + grp.bcast(lp, ll);
+            }
+        } else {
             const int kb = L * M;
             const int ke = min(kb + M, A);
             const int len = ke - kb;
@@ -560,13 +603,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 const int i = i0 + g;
                 float r = 0.0f;
                 if (i < len) {
-                    if (sm.rates) {
-                        r = sm.rates[i * G + L];   // pair kb + i, stored by thread L
-                    } else {
-                        int row, col;
-                        decode_pair(kb + i, h, A1, T1, T2, inv1, inv2, row, col);
-                        r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
-                    }
+                    int row, col;
+                    decode_pair(kb + i, h, A1, T1, T2, inv1, inv2, row, col);
+                    r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
                 }
                 float ctot;
                 const float q = grp.scanf(r, ctot);
