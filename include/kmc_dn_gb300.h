@@ -82,6 +82,35 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
                      int32_t *hop_log, double *time_out, int32_t *status_out,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * kmc_simulate_f64 without a workspace argument, for callers that cannot
+ * allocate device memory at the point of the call: a host application that
+ * owns the device through its own memory pool and passes this library only
+ * the buffers it placed, or a latency-bound loop where cudaMalloc/cudaFree
+ * (which can synchronise the device) are not acceptable.  No counterpart in
+ * the reference (its Go library allocates freely on the host).
+ *   - The workspace is a fixed array inside this library: networks of at
+ *     most 128 sites (N + P); larger ones return KMC_ERR_INVALID with a
+ *     message.  The array (384 KiB) stays resident on every device that
+ *     loads the library until the process exits.
+ *   - The first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress) and caches it; make that first call before any
+ *     stream capture on that device.
+ *   - All calls share the one array: calls whose kernels overlap on the
+ *     device (different streams, or host threads) race and corrupt each
+ *     other's results.  Serialise them on one stream.
+ *   - Everything else (arguments, semantics, asynchrony) is that of
+ *     kmc_simulate_f64.  The call allocates nothing.
+ */
+int kmc_simulate_f64_static(int32_t n_acceptors, int32_t n_electrodes, double nu, double kT,
+                            double I_0, double R, uint8_t *occupation, const double *distances,
+                            const double *E_constant, const double *site_energies,
+                            const double *transitions_constant, int64_t *electrode_occupation,
+                            int64_t hops, int32_t record, double *traffic,
+                            double *occupations_in_time, const double *uniforms, uint64_t seed,
+                            int32_t *hop_log, double *time_out, int32_t *status_out,
+                            void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Batched FP32 engine                                                       */
 /* ------------------------------------------------------------------------ */

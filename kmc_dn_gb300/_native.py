@@ -68,6 +68,8 @@ _SIGS = {
     "kmc_simulate_f64_workspace_size": (_sz, [_i32]),
     "kmc_simulate_f64": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
                                    _i64, _i32, _vp, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "kmc_simulate_f64_static": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp,
+                                          _vp, _i64, _i32, _vp, _vp, _vp, _u64, _vp, _vp, _vp, _vp]),
     "kmc_build_table": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _vp, _vp, _vp, _vp]),
     "kmc_site_energies": (C.c_int, [_i32, _i32, _i32, _vp, _vp, _f64, _vp, _vp, _vp, _vp]),
     "kmc_run_batch": (C.c_int, [C.POINTER(KmcBatch), _vp]),

@@ -20,6 +20,7 @@
 // This is the baseline kernel the batched FP32 engine is measured against,
 // and the kernel of the bit-exact replay check.
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "kmc_common.cuh"
@@ -229,4 +230,79 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
     return KMC_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant
+//
+// Some callers of this kernel cannot allocate device memory when they call
+// it: a host that owns every byte of the device through its own memory pool
+// and hands plugins only the buffers it placed, or a latency-bound loop in
+// which a cudaMalloc / cudaFree (which may synchronise the whole device)
+// would stall other work.  For them the workspace is a fixed array in this
+// library's device memory instead of a caller-provided buffer.
+// ---------------------------------------------------------------------------
+
+// Largest network the static workspace holds: S = N + P <= 128 sites, i.e.
+// 3 * 128^2 doubles = 384 KiB, resident on every device that loads the
+// library until the process exits.
+constexpr int kStaticWorkspaceSites = 128;
+static __device__ __align__(256) double g_f64_static_workspace[3 * kStaticWorkspaceSites * kStaticWorkspaceSites];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_ws_mutex;
+double *g_ws_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the static workspace on the current device.  The array's
+// name is only a host-side stand-in in host code, so the address is looked up
+// once per device (with that device current) and cached.
+static int static_workspace(double **out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_cuda(e, "simulate_f64_static: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(KMC_ERR_INVALID, "simulate_f64_static: device %d beyond the %d this library tracks", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_ws_mutex);
+    if (!g_ws_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_f64_static_workspace);
+        if (e != cudaSuccess) return fail_cuda(e, "simulate_f64_static: cudaGetSymbolAddress");
+        g_ws_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_ws_ptr[dev];
+    return KMC_OK;
+}
+
 }  // namespace kmc
+
+extern "C" int kmc_simulate_f64_static(int32_t n_acceptors, int32_t n_electrodes, double nu,
+                                       double kT, double I_0, double R, uint8_t *occupation,
+                                       const double *distances, const double *E_constant,
+                                       const double *site_energies,
+                                       const double *transitions_constant,
+                                       int64_t *electrode_occupation, int64_t hops, int32_t record,
+                                       double *traffic, double *occupations_in_time,
+                                       const double *uniforms, uint64_t seed, int32_t *hop_log,
+                                       double *time_out, int32_t *status_out, void *stream)
+{
+    using namespace kmc;
+    const int S = n_acceptors + n_electrodes;
+    if (n_acceptors < 0 || n_electrodes < 0 || S <= 0 || S > kStaticWorkspaceSites)
+        return fail(KMC_ERR_INVALID,
+                    "kmc_simulate_f64_static: %d sites (N=%d, P=%d); the fixed workspace holds at most %d "
+                    "(use kmc_simulate_f64 with a caller workspace for larger networks)",
+                    S, n_acceptors, n_electrodes, kStaticWorkspaceSites);
+    double *ws = nullptr;
+    const int rc = static_workspace(&ws);
+    if (rc != KMC_OK) return rc;
+    // The kernel writes every workspace entry it reads within the call
+    // (1/d, I_0 R/d and the running sums), so the contents a previous call
+    // left behind need no clearing.
+    return simulate_f64(n_acceptors, n_electrodes, nu, kT, I_0, R, occupation, distances, E_constant,
+                        site_energies, transitions_constant, electrode_occupation, hops, record,
+                        traffic, occupations_in_time, uniforms, seed, hop_log, time_out, status_out,
+                        ws, sizeof(double) * 3 * (size_t)kStaticWorkspaceSites * kStaticWorkspaceSites,
+                        static_cast<cudaStream_t>(stream));
+}
