@@ -105,22 +105,22 @@ struct TablePairs {
     using Rec = int2;
     const float2 *tab;
     int S;
-    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int S_)
+    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int S_, const float2 *shared_tab)
     {
-        tab = reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
+        tab = shared_tab ? shared_tab : reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
         S = S_;
     }
     __device__ __forceinline__ Rec rec(int site, float e) const { return make_int2(site, __float_as_int(e)); }
     __device__ __forceinline__ float rate(Rec s, Rec t, bool /*acc*/, float cs) const
     {
-        const float2 lb = __ldg(&tab[s.x * S + t.x]);
+        const float2 lb = tab[s.x * S + t.x];
         float x = __int_as_float(t.y) - __int_as_float(s.y);
         x = fmaf(-cs, lb.y, x);
         x = fmaxf(x, 0.0f);
         return ex2_approx(lb.x - x);
     }
     // Coulomb term I_0 R / d_jk between acceptors j, k (0 on the diagonal).
-    __device__ __forceinline__ float coulomb(int j, int k) const { return __ldg(&tab[j * S + k]).y; }
+    __device__ __forceinline__ float coulomb(int j, int k) const { return tab[j * S + k].y; }
 };
 
 // Positions mode: records are {x, y, z, scaled energy}; d from coordinates.
@@ -128,7 +128,7 @@ struct PositionPairs {
     using Rec = float4;
     const float4 *pos;
     float kL, L0, IR;
-    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int /*S*/)
+    __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int /*S*/, const float2 *)
     {
         pos = reinterpret_cast<const float4 *>(B.tab_pos + B.tab_pos_off[t_id]);
         const float4 c = reinterpret_cast<const float4 *>(B.tab_coef)[t_id];
@@ -375,7 +375,7 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_
 
 template <typename Grp, typename Pairs>
 __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename Pairs::Rec> sm,
-                          int c)
+                          int c, const float2 *shared_tab)
 {
     constexpr int G = Grp::kSize;
     using Rec = typename Pairs::Rec;
@@ -389,7 +389,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         return;
     }
     Pairs pairs;
-    pairs.init(B, t_id, S);
+    pairs.init(B, t_id, S, shared_tab);
     const int64_t so = B.chain_site_off[c];
     const int64_t eoff = B.chain_el_off[c];
     const float *Ec = B.E_constant + so;
@@ -697,14 +697,32 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     }
 }
 
+// Stage the one pair table of a launch in shared memory (the whole block).
+__device__ __forceinline__ const float2 *stage_table(const kmc_batch &B, uint32_t *smem, int table_words)
+{
+    if (table_words <= 0) return nullptr;
+    // exactly the table's S*S (L, B) pairs; table_words only rounds the
+    // shared-memory reservation up
+    const int S = B.tab_N[0] + B.tab_P[0];
+    if (S > B.max_sites) return nullptr;   // invalid launch: chains report it
+    const float2 *src = reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[0]);
+    float2 *dst = reinterpret_cast<float2 *>(smem);
+    for (int i = threadIdx.x; i < S * S; i += blockDim.x) dst[i] = __ldg(&src[i]);
+    __syncthreads();
+    return reinterpret_cast<const float2 *>(smem);
+}
+
 // Warp-sliced kernel: 32/G chains per warp, warps_per_block warps.  The
 // bound of 3 blocks of 256 threads keeps registers at or below 85 so that
-// 24 warps fit on an SM.
+// 24 warps fit on an SM.  table_words > 0: every chain of the launch uses
+// table 0, staged in shared memory ahead of the per-chain areas.
 template <int G, typename Pairs>
-__global__ void __launch_bounds__(256, 3) warp_engine_kernel(const kmc_batch B, int rate_words)
+__global__ void __launch_bounds__(256, 3) warp_engine_kernel(const kmc_batch B, int rate_words,
+                                                             int table_words)
 {
     constexpr int CPW = 32 / G;
     extern __shared__ __align__(16) uint32_t smem[];
+    const float2 *stab = stage_table(B, smem, table_words);
     WarpGroup<G> grp;
     grp.init();
     const int warp = threadIdx.x >> 5;
@@ -714,17 +732,20 @@ __global__ void __launch_bounds__(256, 3) warp_engine_kernel(const kmc_batch B, 
     if (c < 0 || c >= B.n_chains) return;   // the whole group leaves together
     using Rec = typename Pairs::Rec;
     const int words = chain_list_words<Rec>(B.max_sites) + rate_words;
-    ChainSmem<Rec> sm = carve<Rec>(smem + (warp * CPW + grp.sub) * words, B.max_sites, rate_words);
-    run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c);
+    ChainSmem<Rec> sm = carve<Rec>(smem + table_words + (warp * CPW + grp.sub) * words, B.max_sites,
+                                   rate_words);
+    run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c, stab);
 }
 
 // Block kernel: one chain per block of T threads.
 template <int T, typename Pairs>
-__global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B, int rate_words)
+__global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B, int rate_words,
+                                                         int table_words)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ double scratch[T / 32 + 2];
     __shared__ int iscratch[2];
+    const float2 *stab = stage_table(B, smem, table_words);
     BlockGroup<T> grp;
     grp.init();
     grp.sd = scratch;
@@ -732,8 +753,8 @@ __global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B, int 
     const int c = B.work[blockIdx.x];
     if (c < 0 || c >= B.n_chains) return;   // uniform over the block
     using Rec = typename Pairs::Rec;
-    ChainSmem<Rec> sm = carve<Rec>(smem, B.max_sites, rate_words);
-    run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c);
+    ChainSmem<Rec> sm = carve<Rec>(smem + table_words, B.max_sites, rate_words);
+    run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c, stab);
 }
 
 template <typename K>
@@ -753,6 +774,16 @@ int set_smem(K kernel, size_t smem, int &configured)
 
 constexpr size_t kSmemBudget = 200 * 1024;   // per block, leaving room for static scratch
 
+// Words of the staged pair table, or 0 when the launch has more than one
+// table (or is not in table mode) or it would not fit next to `rest` bytes.
+template <typename Pairs>
+int table_stage_words(const kmc_batch &b, size_t rest)
+{
+    if (b.pair_mode != KMC_PAIRS_TABLE || b.n_tables != 1) return 0;
+    const size_t w = ((2 * static_cast<size_t>(b.max_sites) * b.max_sites) + 3) & ~static_cast<size_t>(3);
+    return (w * 4 + rest <= kSmemBudget && w * 4 <= 64 * 1024) ? static_cast<int>(w) : 0;
+}
+
 template <int G, typename Pairs>
 int launch_warp(const kmc_batch &b, cudaStream_t st)
 {
@@ -761,7 +792,9 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
     const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
     int rw = rate_buffer_words(b.max_sites, G);
     if (static_cast<size_t>(wpb) * CPW * (lw + rw) * 4 > kSmemBudget) rw = 0;   // recompute instead
-    const size_t smem = static_cast<size_t>(wpb) * CPW * (lw + rw) * 4;
+    const size_t chains = static_cast<size_t>(wpb) * CPW * (lw + rw) * 4;
+    const int tw = table_stage_words<Pairs>(b, chains);
+    const size_t smem = chains + static_cast<size_t>(tw) * 4;
     if (smem > kSmemBudget)
         return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per block (max_sites %d, G %d, %d warps) exceeds the budget",
                     smem, b.max_sites, G, wpb);
@@ -770,7 +803,7 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
     if (rc != KMC_OK) return rc;
     const int grid = (b.n_work + wpb - 1) / wpb;
     if (grid <= 0) return KMC_OK;
-    warp_engine_kernel<G, Pairs><<<grid, wpb * 32, smem, st>>>(b, rw);
+    warp_engine_kernel<G, Pairs><<<grid, wpb * 32, smem, st>>>(b, rw, tw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }
@@ -781,7 +814,9 @@ int launch_block(const kmc_batch &b, cudaStream_t st)
     const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
     int rw = rate_buffer_words(b.max_sites, T);
     if (static_cast<size_t>(lw + rw) * 4 > kSmemBudget) rw = 0;
-    const size_t smem = static_cast<size_t>(lw + rw) * 4;
+    const size_t chain = static_cast<size_t>(lw + rw) * 4;
+    const int tw = table_stage_words<Pairs>(b, chain);
+    const size_t smem = chain + static_cast<size_t>(tw) * 4;
     if (smem > kSmemBudget)
         return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per chain (max_sites %d) exceeds the block budget",
                     smem, b.max_sites);
@@ -789,7 +824,7 @@ int launch_block(const kmc_batch &b, cudaStream_t st)
     const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
     if (rc != KMC_OK) return rc;
     if (b.n_work <= 0) return KMC_OK;
-    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw);
+    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw, tw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }
