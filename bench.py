@@ -131,6 +131,57 @@ def cpu_baseline(net, V, threads, hops, n_chains, budget_s=20.0):
                       f"reference's Go simulate loop, no memo), {dt:.1f} s wall"}
 
 
+def accuracy_of(cases, dev, replicas=16, hops=100_000, seed=0, pair_mode="table"):
+    """Electrode currents of the FP32 engine against the plain FP64 kernel
+    (whose hop sequences equal the reference loop's, bit for bit).
+
+    ``cases``: (network, voltages) pairs; each runs ``replicas`` independent
+    times on both.  Per current: the z-score of the mean difference and,
+    where the standard error resolves it (below 0.25 % of the current), the
+    relative difference."""
+    from kmc_dn_gb300.engine import Batch, TableSpec, simulate_f64_many
+    rows = [c for c in range(len(cases)) for _ in range(replicas)]
+    specs = [TableSpec.from_network(net) if pair_mode == "positions" else
+             TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+             for net, _ in cases]
+    b = Batch(specs, np.array(rows, np.int32), [cases[c][0].kT for c in rows],
+              [cases[c][0].E_constant(cases[c][1]) for c in rows], [cases[c][1] for c in rows],
+              [cases[c][0].occupation.astype(np.uint8) for c in rows], np.full(len(rows), hops),
+              streams=np.arange(len(rows)) + 10_000_000, seed=seed + 101, dev=dev, pair_mode=pair_mode)
+    r32 = b.run().results()
+    assert np.all(r32["status"] == 0)
+    chains = [dict(N=n.N, P=n.P, nu=n.nu, kT=n.kT, I_0=n.I_0, R=n.R, occupation=n.occupation,
+                   distances=n.distances, E_constant=n.E_constant(v), site_energies=n.site_energies(v),
+                   transitions_constant=n.transitions_constant) for n, v in (cases[c] for c in rows)]
+    t64, eo64, st64 = simulate_f64_many(chains, hops, [seed * 7919 + 13 + i for i in range(len(rows))], dev=dev)
+    assert np.all(st64 == 0)
+    zs, rels, res = [], [], []
+    for c in range(len(cases)):
+        idx = [i for i, rc in enumerate(rows) if rc == c]
+        I32 = np.stack([r32["electrode_occupation"][i] / r32["time"][i] for i in idx])
+        I64 = np.stack([eo64[i] / t64[i] for i in idx])
+        m32, m64 = I32.mean(0), I64.mean(0)
+        se = np.sqrt(I32.var(0, ddof=1) / replicas + I64.var(0, ddof=1) / replicas)
+        zs.append(np.abs(m32 - m64) / np.maximum(se, 1e-300))
+        rels.append(np.abs(m32 - m64) / np.maximum(np.abs(m64), 1e-300))
+        res.append(se < 0.0025 * np.abs(m64))
+    z, rel, resolved = np.concatenate(zs), np.concatenate(rels), np.concatenate(res)
+    return {"currents": int(z.size), "chains": len(cases), "replicas": replicas, "hops": hops,
+            "max_abs_z": float(z.max()), "frac_within_3sigma": float(np.mean(z <= 3.0)),
+            "resolved_currents": int(resolved.sum()),
+            "max_rel_err_resolved": float(rel[resolved].max()) if resolved.any() else None,
+            "frac_resolved_within_1pct": float(np.mean(rel[resolved] <= 0.01)) if resolved.any() else None}
+
+
+def accuracy_sample(net, V, dev, n_chains=4, replicas=16, hops=100_000, seed=0):
+    """``accuracy_of`` on the first ``n_chains`` voltage vectors of the
+    homogeneous workload."""
+    out = accuracy_of([(net, V[k]) for k in range(n_chains)], dev, replicas, hops, seed)
+    out["reference"] = ("plain FP64 kernel (bit-exact to the reference loop's hop sequence), "
+                        "independent replicas")
+    return out
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -169,10 +220,28 @@ def main():
     ap.add_argument("--warps-per-block", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--workload", default="homogeneous",
+                    choices=["homogeneous", "uneven", "large", "serving", "meanfield"],
+                    help="homogeneous: the headline line; the others measure the other "
+                         "workloads of the path (one JSON line each)")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--drain-seconds", type=float, default=120.0)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.workload != "homogeneous":
+        import __graft_entry__
+        __graft_entry__.build()
+        import torch
+        torch.cuda.set_device(local)
+        fn = {"uneven": bench_uneven, "large": bench_large, "serving": bench_serving,
+              "meanfield": bench_meanfield}[args.workload]
+        if rank == 0:
+            print(json.dumps(fn(args)), flush=True)
+        return
 
     import torch
     import __graft_entry__
@@ -285,6 +354,10 @@ def main():
         if not args.no_e2e:
             e2e = run_e2e(net, V, hops, args.seed + 1, lanes or 0)
 
+        acc = None
+        if not args.no_accuracy:
+            acc = accuracy_sample(net, V, dev, seed=args.seed)
+
         cpu = None
         if not args.no_cpu_baseline and world == 1:
             cpu = cpu_baseline(net, V, os.cpu_count() or 1, hops, min(256, n_chains))
@@ -303,6 +376,7 @@ def main():
                             "unit": "Gexp/s", "frac": achieved / peak.value, "traffic": traffic,
                             "peak_source": "ex2.approx throughput measured live (kmc_measure_ex2_rate)",
                             "work": "allowed pairs A(h) summed over all hops of a launch, one ex2 each"},
+               "accuracy_vs_fp64": acc,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": launches_per_step * args.steps,
                "wall_s": wall}
@@ -354,6 +428,229 @@ def run_e2e(net, V, hops, seed, lanes):
     d2h = t_out.nbytes + eo.nbytes + occ.nbytes + st.nbytes
     return {"value": n * hops / dt, "unit": "hops/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "api": "kmc_run_batch_host (C ABI, host buffers)"}
+
+
+def _timed_launch(b, hops, streams):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for st in streams:
+        st.wait_event(e0)
+    b.launch(hops, bin_streams=streams)
+    for st in streams:
+        ev = torch.cuda.Event()
+        ev.record(st)
+        torch.cuda.current_stream().wait_event(ev)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def bench_uneven(args):
+    """16384 chains, one network each: N ~ U{10..200}, M = 0.1 N, P ~ U{4..12},
+    kT log-uniform [0.5, 5], ab/R ~ U[0.5, 2], V ~ U[-2, 2], hops log-uniform
+    [1e4, 1e6]; size bins run side by side on their own streams."""
+    import torch
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = args.chains if args.chains != N_CHAINS else 16384
+    t0 = time.perf_counter()
+    nets = workloads.uneven_batch(n, seed=args.seed)
+    setup_s = time.perf_counter() - t0
+    specs = [TableSpec.from_network(net) for net, _ in nets]
+    hops = np.array([h for _, h in nets], np.int64)
+    b = Batch(specs, np.arange(n), [net.kT for net, _ in nets], [net.E_constant() for net, _ in nets],
+              [net.electrodes[:, 3] for net, _ in nets], [net.occupation.astype(np.uint8) for net, _ in nets],
+              hops, seed=args.seed + 5, pair_mode="positions")
+    streams = [torch.cuda.Stream() for _ in range(len(b._bins))]
+    dt = _timed_launch(b, int(hops.max()), streams)
+    r = b.results()
+    assert np.all(r["status"] == 0)
+    done = int(r["hops_done"].sum())
+    S = np.array([s.S for s in specs])
+    bins = []
+    for bn in b._bins:
+        idx = bn["chains"]
+        bins.append({"lanes_per_chain": bn["G"], "chains": int(len(idx)), "S_range": [int(S[idx].min()), int(S[idx].max())],
+                     "hops": int(r["hops_done"][idx].sum())})
+    if not args.no_accuracy:
+        # FP32 vs FP64 currents per size bin: two networks of each bin, 16
+        # replicas each on both kernels (fewer hops for the large bins: the
+        # FP64 kernel costs O(S^2) FP64 work per hop)
+        for bn, entry in zip(b._bins, bins):
+            idx = list(bn["chains"][:2])
+            smax = int(S[idx].max())
+            ah = 100_000 if smax <= 64 else 30_000 if smax <= 128 else 10_000
+            entry["accuracy_vs_fp64"] = accuracy_of([(nets[i][0], nets[i][0].electrodes[:, 3]) for i in idx],
+                                                    torch.device("cuda"), hops=ah, seed=args.seed + 3,
+                                                    pair_mode="positions")
+    return {"metric": METRIC, "value": done / dt, "unit": "hops/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uneven batch: 16384 chains, one network each, N~U{10..200}, P~U{4..12}, "
+                                   "hops log-uniform [1e4,1e6]", "n_chains": n, "total_hops": done,
+                       "pair_mode": "positions", "bins": bins, "host_setup_s": setup_s},
+            "gpu_launches": len(b._bins), "n_pairs_per_s": float(r["n_pairs"].sum()) / dt}
+
+
+def bench_large(args):
+    """256 chains on their own N=1000, M=100 networks (20x20 density, 8
+    electrodes, V ~ U[-1,1]), block groups, positions mode."""
+    import torch
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = 256 if args.chains == N_CHAINS else args.chains
+    hops = args.hops if args.hops != HOPS else 100_000
+    nets = [workloads.large_network(seed=1000 + i) for i in range(n)]
+    specs = [TableSpec.from_network(net) for net in nets]
+    lanes = args.lanes or 256
+    b = Batch(specs, np.arange(n), [1.0] * n, [net.E_constant() for net in nets],
+              [net.electrodes[:, 3] for net in nets], [net.occupation.astype(np.uint8) for net in nets],
+              [10**12] * n, seed=args.seed + 9, pair_mode="positions", lanes=lanes)
+    b.launch(1024)
+    torch.cuda.synchronize()
+    b.n_pairs.zero_()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.launch(hops)
+    e1.record()
+    e1.synchronize()
+    dt = e0.elapsed_time(e1) * 1e-3
+    r = b.results()
+    assert np.all(r["status"] == 0)
+    peak = C.c_double(0)
+    from kmc_dn_gb300 import _native
+    _native.check(_native.lib().kmc_measure_ex2_rate(C.byref(peak)))
+    pairs = float(r["n_pairs"].sum())
+    return {"metric": METRIC, "value": n * hops / dt, "unit": "hops/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "large networks: 256 chains, own N=1000 M=100 networks, 8 electrodes",
+                       "n_chains": n, "hops_per_chain_timed": hops, "lanes_per_chain": lanes,
+                       "pair_mode": "positions"},
+            "roofline": {"bound": "sfu", "achieved": pairs / dt / 1e9, "peak": peak.value / 1e9,
+                         "unit": "Gexp/s", "frac": pairs / dt / peak.value,
+                         "work": "allowed pairs (one ex2 and one rsqrt each in positions mode)"},
+            "gpu_launches": 1}
+
+
+def bench_meanfield(args):
+    """Mean-field relaxation (Go probSimulate) of 4096 networks: the N=30,
+    P=8 geometry with each network's own voltage vector, 1000 iterations
+    each (dn_search's first search stage), FP32 and FP64 rates; the C
+    restatement of the Go function on all host threads beside it."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    from kmc_dn_gb300 import _native
+    from kmc_dn_gb300.meanfield import MeanFieldBatch, Network
+    n = args.chains if args.chains != N_CHAINS else 4096
+    iters = 1000
+    net, V = build_workload(args.seed, n)
+    nets = [Network(net.N, net.P, net.nu, net.kT, net.I_0, net.R, net.distances, net.transitions_constant,
+                    net.E_constant(V[k]), V[k]) for k in range(n)]
+    out = {}
+    for rates in ("f32", "f64"):
+        b = MeanFieldBatch(nets, iters, rates=rates)
+        st = torch.cuda.Stream()
+        with torch.cuda.stream(st):
+            for _ in range(max(1, args.warmup)):
+                b.reset()
+                b.launch(st)
+        st.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(st):
+                b.reset()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                b.launch(st)
+                e1.record(st)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        r = b.results()
+        assert np.all(r["status"] == 0) and np.all(r["iterations"] == iters)
+        t = float(np.mean(ms)) * 1e-3
+        out[rates] = {"network_iterations_per_s": n * iters / t, "ms_per_launch": t * 1e3,
+                      "pairs_per_s": b.pairs_per_iteration * iters / t}
+    peak = C.c_double(0)
+    _native.check(_native.lib().kmc_measure_ex2_rate(C.byref(peak)))
+    # CPU: the oracle's restatement of probSimulate, one network per task
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle as orc
+    threads = os.cpu_count() or 1
+    k = max(threads, 32)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda i: orc.prob_simulate(net.N, net.P, net.nu, net.kT, net.I_0, net.R, np.full(net.N, 0.5),
+                                                net.distances, net.E_constant(V[i]), net.site_energies(V[i]),
+                                                net.transitions_constant, iters), range(k)))
+    cpu_dt = time.perf_counter() - t0
+    f32 = out["f32"]
+    return {"metric": "mean-field network-iterations/s", "value": f32["network_iterations_per_s"],
+            "unit": "network-iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": f32["ms_per_launch"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 rates, f64 state", "data": "synthetic",
+            "config": {"workload": f"mean-field relaxation: {n} networks (N=30, P=8, own voltages) x {iters} "
+                                   "iterations", "n_networks": n, "iterations": iters,
+                       "l2": "inputs resident (a few MB), not flushed"},
+            "fp64_rates": out["f64"],
+            "roofline": {"bound": "sfu", "achieved": f32["pairs_per_s"] / 1e9, "peak": peak.value / 1e9,
+                         "unit": "Gexp/s", "frac": f32["pairs_per_s"] / peak.value,
+                         "work": "S*S pair rates per network-iteration, one ex2 each"},
+            "cpu_baseline": {"value": k * iters / cpu_dt, "unit": "network-iterations/s", "cores": threads,
+                             "kind": "port", "sample": f"{k} networks x {iters} iterations, C restatement "
+                                                       f"of probSimulate, {cpu_dt:.1f} s wall"},
+            "gpu_launches": args.steps}
+
+
+def bench_serving(args):
+    """Poisson arrivals (args.rate per second for args.serve_seconds) of
+    voltage populations (32..512 vectors, U[-1,1]) on 4 resident geometries
+    (N in {30, 60, 120, 240}, M = 0.1 N, 8 electrodes), hop budgets from
+    {1e4, 1e5, 1e6}; continuous batching; p50/p99 latency per budget."""
+    import threading
+    import torch
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.serving import Server, latency_summary
+    nets = workloads.serving_geometries(seed=args.seed)
+    srv = Server(nets, quantum=4096, n_streams=8)
+    rng = np.random.Generator(np.random.PCG64(args.seed + 77))
+    n_req = rng.poisson(args.rate * args.serve_seconds)
+    gaps = rng.exponential(1.0 / args.rate, n_req)
+    arr = np.cumsum(gaps)
+    reqs_spec = [(int(rng.integers(4)), rng.uniform(-1, 1, (int(rng.integers(32, 513)), 8)),
+                  int(rng.choice([10_000, 100_000, 1_000_000])), int(rng.integers(2**62))) for _ in range(n_req)]
+    # warm-up: one small request per geometry (module load, allocator pools)
+    for g in range(4):
+        srv.submit(g, np.zeros((32, 8)), 2048, seed=g)
+    srv.run_sync()
+    srv.finished.clear()
+    srv.hops_done = 0
+    srv.start()
+    submitted = []
+    t0 = time.perf_counter()
+    for (g, V, h, sd), ta in zip(reqs_spec, arr):
+        delay = t0 + ta - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        submitted.append(srv.submit(g, V, h, sd))
+    drained = srv.wait_idle(timeout=args.drain_seconds)
+    wall = time.perf_counter() - t0
+    srv.stop(drain=False)
+    done = [r for r in submitted if r.done_at is not None]
+    lat = latency_summary(done)
+    return {"metric": METRIC, "value": srv.hops_done / wall, "unit": "hops/s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serving: Poisson voltage-search requests on 4 resident geometries",
+                       "rate_per_s": args.rate, "arrival_window_s": args.serve_seconds,
+                       "requests": int(n_req), "completed": len(done), "drained": bool(drained),
+                       "quantum_hops": 4096},
+            "latency": lat, "gpu_launches": None}
 
 
 if __name__ == "__main__":

@@ -267,6 +267,95 @@ int kmc_run_batch_host(int32_t n_geoms, const int32_t *geom_N, const int32_t *ge
                        int32_t lanes_per_chain, double *time_out,
                        int64_t *electrode_occupation, int32_t *status);
 
+/* ------------------------------------------------------------------------ */
+/* Mean-field relaxation (replaces probSimulate / wrapperSimulateProbability, */
+/* goSimulation/probabilitySimulation.go:53-157, simulationWrapper.go:224-235) */
+/* ------------------------------------------------------------------------ */
+
+#define KMC_MF_RATES_F64 0   /* exp() in FP64: the reference's arithmetic       */
+#define KMC_MF_RATES_F32 1   /* ex2.approx.f32 rates, FP64 sums and state       */
+
+/*
+ * One network per chain; every pointer is a device pointer for kmc_mf_run and
+ * a host pointer for kmc_mf_run_host.  Per-chain segments:
+ *   pair_off[c]    S*S row-major block of distances / transitions_constant
+ *                  (chains may share a block),
+ *   site_off[c]    S-entry segment of E_constant (first N used),
+ *                  site_energies (in: entries N..S-1 = electrode voltages;
+ *                  out: entries 0..N-1 = the last iteration's energies),
+ *                  occupation (first N: start probabilities in, final out)
+ *                  and average_occupation (record: first N, time-weighted
+ *                  probability sums, accumulated),
+ *   el_off[c]      P entries of electrode_occupation (out: integrated net
+ *                  expected charge into each electrode; the Go function
+ *                  zeroes it first),
+ *   traffic_off[c] S*S block of traffic (record: net expected flow i->j,
+ *                  accumulated onto the caller's values).
+ * time[c] receives the simulated time, status[c] KMC_OK or
+ * KMC_ERR_NONFINITE (total rate zero or non-finite: the chain stops where
+ * the Go loop would produce NaN), iterations_done[c] the iterations run.
+ */
+typedef struct kmc_mf_batch {
+    int32_t n_chains;
+    int32_t max_sites;              /* >= S of every chain, <= kmc_mf_max_sites */
+    int32_t rates;                  /* KMC_MF_RATES_*                          */
+    int32_t record;                 /* 0 / 1                                   */
+    const int32_t *N;               /* [n_chains]                              */
+    const int32_t *P;
+    const double *nu, *kT, *I_0, *R;
+    const int64_t *pair_off;
+    const double *distances;
+    const double *transitions_constant;
+    const int64_t *site_off;
+    const double *E_constant;
+    double *site_energies;
+    double *occupation;
+    const int64_t *el_off;
+    double *electrode_occupation;
+    const int64_t *hops;            /* [n_chains] iterations (the Go "hops")   */
+    const int64_t *traffic_off;     /* record only                             */
+    double *traffic;
+    double *average_occupation;
+    double *time;                   /* [n_chains]                              */
+    int32_t *status;                /* [n_chains] or NULL                      */
+    int64_t *iterations_done;       /* [n_chains] or NULL                      */
+} kmc_mf_batch;
+
+/* Largest S a chain may have for the given rate precision (its tables and
+ * rates stay in one block's shared memory). */
+int32_t kmc_mf_max_sites(int32_t rates);
+/* Dynamic shared memory one block of kmc_mf_run uses. */
+size_t kmc_mf_smem_bytes(int32_t max_sites, int32_t rates);
+/* Device pointers, asynchronous on `stream`. */
+int kmc_mf_run(const kmc_mf_batch *batch, void *stream);
+/* Host pointers: copies in, runs, copies out, synchronises. */
+int kmc_mf_run_host(const kmc_mf_batch *batch, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Laplace basis fields on the device                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Workspace bytes of kmc_laplace_basis for an nx x ny-cell mesh, n fields. */
+size_t kmc_laplace_workspace_size(int32_t nx, int32_t ny, int32_t n_fields);
+
+/*
+ * Solve the Laplace problem of the reference's potential set-up (P1 elements
+ * on a uniform right-triangle mesh with Dirichlet data on the whole boundary,
+ * init_V/update_V, kmc_dopant_networks.py:706-822) for n_fields boundary
+ * data sets at once.  grid (device, n_fields x (ny+1) x (nx+1), row = y
+ * index) carries each field's boundary values on entry; its interior is
+ * overwritten with the solution.  Exact direct solve by sine transforms.
+ */
+int kmc_laplace_basis(int32_t nx, int32_t ny, double hx, double hy, int32_t n_fields,
+                      double *grid, void *workspace, size_t workspace_bytes, void *stream);
+
+/* P1 interpolation of n_fields nodal grids at n_points (x, y) points
+ * (device xy[2*n_points]); out[f*n_points + p].  The point evaluation of the
+ * FEniCS function V(x, y) (kmc_dopant_networks.py:851-853). */
+int kmc_p1_sample(int32_t nx, int32_t ny, double hx, double hy, int32_t n_fields,
+                  const double *grid, int32_t n_points, const double *xy, double *out,
+                  void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,19 @@ double wrapperSimulatePruned(int64_t NSites, int64_t NElectrodes, double prune_t
                              GoSlice electrode_occupation, GoSlice site_energies, int hops,
                              uint8_t record, GoSlice traffic, GoSlice average_occupation);
 
+/* goSimulation/simulationWrapper.go:224-235: mean-field relaxation
+ * (probSimulate, probabilitySimulation.go:53-157) from occupation 0.5 on
+ * every acceptor.  Writes occupation (the final probabilities),
+ * electrode_occupation (integrated net expected charge), site_energies
+ * (acceptor entries) and, with record, traffic / average_occupation
+ * (accumulated, as the Go function does).  FP64 arithmetic.  Returns the
+ * simulated time, or a negative KMC_ERR_* code. */
+double wrapperSimulateProbability(int64_t NSites, int64_t NElectrodes, double nu, double kT,
+                                  double I_0, double R, GoSlice occupation, GoSlice distances,
+                                  GoSlice E_constant, GoSlice transitions_constant,
+                                  GoSlice electrode_occupation, GoSlice site_energies, int hops,
+                                  uint8_t record, GoSlice traffic, GoSlice average_occupation);
+
 /* goSimulation/simulationWrapper.go:274-315: ragged batch, one chain per entry,
  * each starting from its own occupation; writes electrode_occupation and time. */
 int64_t parallelSimulations(GoSlice NSites, GoSlice NElectrodes, GoSlice nu, GoSlice kT,

@@ -14,7 +14,7 @@ __all__ = ["lib", "check", "KmcError", "NativeLibraryError", "KmcBatch", "LIB_PA
            "KMC_OK", "KMC_ERR_INVALID", "KMC_ERR_CUDA", "KMC_ERR_OOM", "KMC_ERR_TIMEOUT",
            "KMC_ERR_NONFINITE", "KMC_ERR_CANCELLED", "RECORD_NONE", "RECORD_NUMBA", "RECORD_GO",
            "PAIRS_TABLE", "PAIRS_POSITIONS",
-           "EXPORTED"]
+           "EXPORTED", "KmcMfBatch", "MF_RATES_F64", "MF_RATES_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libkmc_dn_gb300.so")
@@ -28,6 +28,7 @@ KMC_ERR_NONFINITE = -5
 KMC_ERR_CANCELLED = -6
 RECORD_NONE, RECORD_NUMBA, RECORD_GO = 0, 1, 2
 PAIRS_TABLE, PAIRS_POSITIONS = 0, 1
+MF_RATES_F64, MF_RATES_F32 = 0, 1
 
 _vp = C.c_void_p
 _i32, _i64, _u64, _f64, _sz = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_size_t
@@ -61,6 +62,20 @@ class KmcBatch(C.Structure):
     ]
 
 
+class KmcMfBatch(C.Structure):
+    """Mirror of ``struct kmc_mf_batch`` (device addresses for kmc_mf_run,
+    host addresses for kmc_mf_run_host)."""
+    _fields_ = [
+        ("n_chains", _i32), ("max_sites", _i32), ("rates", _i32), ("record", _i32),
+        ("N", _vp), ("P", _vp), ("nu", _vp), ("kT", _vp), ("I_0", _vp), ("R", _vp),
+        ("pair_off", _vp), ("distances", _vp), ("transitions_constant", _vp),
+        ("site_off", _vp), ("E_constant", _vp), ("site_energies", _vp), ("occupation", _vp),
+        ("el_off", _vp), ("electrode_occupation", _vp), ("hops", _vp),
+        ("traffic_off", _vp), ("traffic", _vp), ("average_occupation", _vp),
+        ("time", _vp), ("status", _vp), ("iterations_done", _vp),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/kmc_dn_gb300.h declares
 _SIGS = {
     "kmc_version": (C.c_int, []),
@@ -77,6 +92,13 @@ _SIGS = {
     "kmc_measure_ex2_rate": (C.c_int, [C.POINTER(_f64)]),
     "kmc_run_batch_host": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _u64, _i32, _vp, _vp, _vp]),
+    "kmc_mf_max_sites": (_i32, [_i32]),
+    "kmc_mf_smem_bytes": (_sz, [_i32, _i32]),
+    "kmc_mf_run": (C.c_int, [C.POINTER(KmcMfBatch), _vp]),
+    "kmc_mf_run_host": (C.c_int, [C.POINTER(KmcMfBatch), _vp]),
+    "kmc_laplace_workspace_size": (_sz, [_i32, _i32, _i32]),
+    "kmc_laplace_basis": (C.c_int, [_i32, _i32, _f64, _f64, _i32, _vp, _vp, _sz, _vp]),
+    "kmc_p1_sample": (C.c_int, [_i32, _i32, _f64, _f64, _i32, _vp, _i32, _vp, _vp, _vp]),
 }
 EXPORTED = tuple(_SIGS)
 

@@ -103,6 +103,8 @@ __device__ __forceinline__ void decode_pair(int k, int h, int A1, int T1, int T2
 // Table mode: records are {site, scaled energy}; (L, B) read from the table.
 struct TablePairs {
     using Rec = int2;
+    static constexpr bool kSiteInRec = true;    // rec.x is the site id
+    __device__ __forceinline__ static int site(Rec r) { return r.x; }
     const float2 *tab;
     int S;
     __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int S_, const float2 *shared_tab)
@@ -126,6 +128,8 @@ struct TablePairs {
 // Positions mode: records are {x, y, z, scaled energy}; d from coordinates.
 struct PositionPairs {
     using Rec = float4;
+    static constexpr bool kSiteInRec = false;   // site ids kept beside the records
+    __device__ __forceinline__ static int site(Rec) { return -1; }
     const float4 *pos;
     float kL, L0, IR;
     __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int /*S*/, const float2 *)
@@ -450,23 +454,32 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             const uint32_t word = sm.occw[w];
             const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
             const Rec r = pairs.rec(j, cs * sm.E[j]);
-            if ((word >> (j & 31)) & 1u) { sm.src[below] = r; sm.src_id[below] = j; }
-            else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
+            if ((word >> (j & 31)) & 1u) {
+                sm.src[below] = r;
+                if (!Pairs::kSiteInRec) sm.src_id[below] = j;
+            } else {
+                sm.tgt[j - below] = r;
+                if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
+            }
         }
         for (int e = g; e < P; e += G) {
             const Rec r = pairs.rec(N + e, cs * Vel[e]);
             sm.src[h + e] = r;
-            sm.src_id[h + e] = N + e;
             sm.tgt[z + e] = r;
-            sm.tgt_id[z + e] = N + e;
+            if (!Pairs::kSiteInRec) {
+                sm.src_id[h + e] = N + e;
+                sm.tgt_id[z + e] = N + e;
+            }
         }
         grp.sync();
     };
     anchor_and_build();
     int until_anchor = reanchor - static_cast<int>(hop % reanchor);
 
-    // Philox words: thread g holds the draw of hop rbase + (g mod 32)
-    u32x4 rnd{0, 0, 0, 0};
+    // Thread g holds the two uniforms of hop rbase + (g mod 32), already
+    // mapped: the clock's Exp(1) variate and the event uniform.
+    float rnd_e1 = 0.0f;
+    double rnd_u = 0.0;
     int64_t rbase = INT64_MIN / 2;
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
 
@@ -549,16 +562,16 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             if (hop - rbase >= RW) {
                 rbase = hop;
                 const uint64_t ctr = static_cast<uint64_t>(hop + (g & 31));
-                rnd = philox4x32_10(u32x4{static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
-                                          static_cast<uint32_t>(stream), static_cast<uint32_t>(stream >> 32)},
-                                    k0, k1);
+                const u32x4 w = philox4x32_10(u32x4{static_cast<uint32_t>(ctr), static_cast<uint32_t>(ctr >> 32),
+                                                    static_cast<uint32_t>(stream),
+                                                    static_cast<uint32_t>(stream >> 32)},
+                                              k0, k1);
+                rnd_e1 = -__logf(u01_from32(w.x));
+                rnd_u = u01_from52(w.y, w.z);
             }
             const int ri = static_cast<int>(hop - rbase);
-            const uint32_t w0 = grp.bcast(rnd.x, ri);
-            const uint32_t w1 = grp.bcast(rnd.y, ri);
-            const uint32_t w2 = grp.bcast(rnd.z, ri);
-            e1 = -__logf(u01_from32(w0));
-            u_ev = u01_from52(w1, w2);
+            e1 = grp.bcast(rnd_e1, ri);
+            u_ev = grp.bcast(rnd_u, ri);
         }
         if (sm.rates) grp.sync();   // stored rates visible to the whole group
         // ---- FP64 scan of the per-thread sums ----
@@ -621,8 +634,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (chosen < 0) { status = KMC_ERR_NONFINITE; break; }
         int row, col;
         decode_pair(chosen, h, A1, T1, T2, inv1, inv2, row, col);
-        const int from = sm.src_id[row];
-        const int to = sm.tgt_id[col];
+        const int from = Pairs::kSiteInRec ? Pairs::site(sm.src[row]) : sm.src_id[row];
+        const int to = Pairs::kSiteInRec ? Pairs::site(sm.tgt[col]) : sm.tgt_id[col];
         // ---- clock ----
         const float dt = e1 * __frcp_rn(static_cast<float>(tot));
         const double t_before = t;
@@ -647,16 +660,21 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                                   - ((fa && from < j) ? 1 : 0) + ((tb && to < j) ? 1 : 0);
                 const bool occ_j = (j == to && tb) || (j != from && ((word >> (j & 31)) & 1u));
                 const Rec r = pairs.rec(j, cs * Ej);
-                if (occ_j) { sm.src[below] = r; sm.src_id[below] = j; }
-                else { sm.tgt[j - below] = r; sm.tgt_id[j - below] = j; }
+                if (occ_j) {
+                    sm.src[below] = r;
+                    if (!Pairs::kSiteInRec) sm.src_id[below] = j;
+                } else {
+                    sm.tgt[j - below] = r;
+                    if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
+                }
             }
             if (h_new != h) {
                 for (int e = g; e < P; e += G) {
                     const Rec r = pairs.rec(N + e, cs * Vel[e]);
                     sm.src[h_new + e] = r;
-                    sm.src_id[h_new + e] = N + e;
+                    if (!Pairs::kSiteInRec) sm.src_id[h_new + e] = N + e;
                     sm.tgt[z_new + e] = r;
-                    sm.tgt_id[z_new + e] = N + e;
+                    if (!Pairs::kSiteInRec) sm.tgt_id[z_new + e] = N + e;
                 }
             }
         }

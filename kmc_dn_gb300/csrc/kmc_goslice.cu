@@ -135,6 +135,54 @@ double wrapperSimulatePruned(int64_t NSites, int64_t NElectrodes, double prune_t
                         traffic, average_occupation);
 }
 
+double wrapperSimulateProbability(int64_t NSites, int64_t NElectrodes, double nu, double kT,
+                                  double I_0, double R, GoSlice occupation, GoSlice distances,
+                                  GoSlice E_constant, GoSlice transitions_constant,
+                                  GoSlice electrode_occupation, GoSlice site_energies, int hops,
+                                  uint8_t record, GoSlice traffic, GoSlice average_occupation)
+{
+    using namespace kmc;
+    const int N = static_cast<int>(NSites), P = static_cast<int>(NElectrodes);
+    const int64_t S = (int64_t)N + P;
+    if (N < 0 || P < 0 || S <= 0 || hops < 0 || occupation.len < N || distances.len < S * S ||
+        transitions_constant.len < S * S || E_constant.len < N || site_energies.len < S ||
+        electrode_occupation.len < P || (record && (traffic.len < S * S || average_occupation.len < N)))
+        return fail(KMC_ERR_INVALID, "wrapperSimulateProbability: slice lengths do not match N=%d P=%d", N, P);
+    if (S > kmc_mf_max_sites(KMC_MF_RATES_F64))
+        return fail(KMC_ERR_INVALID, "wrapperSimulateProbability: %lld sites exceed the limit %d",
+                    (long long)S, kmc_mf_max_sites(KMC_MF_RATES_F64));
+    // segments of S entries (simulationWrapper.go:229-232 sets every acceptor to 0.5)
+    std::vector<double> occ(S, 0.0), ec(S, 0.0), se(site_energies.data, site_energies.data + S), avg(S, 0.0);
+    for (int i = 0; i < N; ++i) { occ[i] = 0.5; ec[i] = E_constant.data[i]; }
+    if (record) for (int i = 0; i < N; ++i) avg[i] = average_occupation.data[i];
+    std::vector<double> eo(std::max(P, 1), 0.0);
+    const int32_t n32 = N, p32 = P;
+    const int64_t zero = 0, h = hops;
+    double t = 0.0;
+    int32_t st = 0;
+    int64_t done = 0;
+    kmc_mf_batch b;
+    memset(&b, 0, sizeof(b));
+    b.n_chains = 1;
+    b.max_sites = static_cast<int32_t>(S);
+    b.rates = KMC_MF_RATES_F64;
+    b.record = record ? 1 : 0;
+    b.N = &n32; b.P = &p32; b.nu = &nu; b.kT = &kT; b.I_0 = &I_0; b.R = &R;
+    b.pair_off = &zero; b.distances = distances.data; b.transitions_constant = transitions_constant.data;
+    b.site_off = &zero; b.E_constant = ec.data(); b.site_energies = se.data(); b.occupation = occ.data();
+    b.el_off = &zero; b.electrode_occupation = eo.data(); b.hops = &h;
+    b.traffic_off = &zero; b.traffic = record ? traffic.data : nullptr;
+    b.average_occupation = record ? avg.data() : nullptr;
+    b.time = &t; b.status = &st; b.iterations_done = &done;
+    const int rc = kmc_mf_run_host(&b, nullptr);
+    if (rc != KMC_OK) return rc;
+    if (st != KMC_OK) return fail(st, "wrapperSimulateProbability: total rate zero or non-finite");
+    for (int i = 0; i < N; ++i) { occupation.data[i] = occ[i]; site_energies.data[i] = se[i]; }
+    for (int e = 0; e < P; ++e) electrode_occupation.data[e] = eo[e];
+    if (record) for (int i = 0; i < N; ++i) average_occupation.data[i] = avg[i];
+    return t;
+}
+
 int64_t parallelSimulations(GoSlice NSites, GoSlice NElectrodes, GoSlice nu, GoSlice kT,
                             GoSlice I_0, GoSlice R, GoSlice occupation, GoSlice distances,
                             GoSlice E_constant, GoSlice transitions_constant,

@@ -100,6 +100,47 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     return out
 
 
+def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None):
+    """Run independent FP64 chains concurrently (one kernel launch per chain,
+    spread over ``n_streams`` CUDA streams), for FP64 reference statistics.
+
+    ``chains``: list of dicts with N, P, nu, kT, I_0, R, occupation,
+    distances, E_constant, site_energies, transitions_constant.  Returns
+    (time[C], electrode_occupation[C][P], status[C])."""
+    d = device(dev)
+    f64 = torch.float64
+    L = lib()
+    streams = [torch.cuda.Stream(d) for _ in range(max(1, min(n_streams, len(chains))))]
+    keep, outs = [], []
+    torch.cuda.synchronize(d)
+    for k, (ch, seed) in enumerate(zip(chains, seeds)):
+        N, P = int(ch["N"]), int(ch["P"])
+        S = N + P
+        st = streams[k % len(streams)]
+        with torch.cuda.stream(st):
+            occ = _dev(np.asarray(ch["occupation"], np.uint8).reshape(N), torch.uint8, d)
+            dist = _dev(np.asarray(ch["distances"], np.float64).reshape(S, S), f64, d)
+            tc = _dev(np.asarray(ch["transitions_constant"], np.float64).reshape(S, S), f64, d)
+            ec = _dev(np.asarray(ch["E_constant"], np.float64).reshape(N), f64, d)
+            se = _dev(np.asarray(ch["site_energies"], np.float64).reshape(S), f64, d)
+            eo = torch.zeros(max(P, 1), dtype=torch.int64, device=d)
+            t_out = torch.zeros(1, dtype=f64, device=d)
+            s_out = torch.zeros(1, dtype=torch.int32, device=d)
+            wsb = L.kmc_simulate_f64_workspace_size(S)
+            ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
+        check(L.kmc_simulate_f64(N, P, float(ch["nu"]), float(ch["kT"]), float(ch["I_0"]), float(ch["R"]),
+                                 _ptr(occ), _ptr(dist), _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), int(hops), 0,
+                                 None, None, None, int(seed) & (2**64 - 1), None, _ptr(t_out), _ptr(s_out),
+                                 _ptr(ws), wsb, _stream_handle(st)))
+        keep.append((occ, dist, tc, ec, se, ws))
+        outs.append((t_out, eo, s_out, P))
+    torch.cuda.synchronize(d)
+    times = np.array([float(t.item()) for t, _, _, _ in outs])
+    eos = [e.cpu().numpy()[:P] for _, e, _, P in outs]
+    status = np.array([int(s.item()) for _, _, s, _ in outs])
+    return times, eos, status
+
+
 # ---------------------------------------------------------------------------
 # batched FP32 engine
 # ---------------------------------------------------------------------------
@@ -123,6 +164,7 @@ class TableSpec:
     transitions_constant: np.ndarray
     positions: Optional[np.ndarray] = None
     ab: Optional[float] = None
+    from_positions: bool = False      # tables computed from `positions` by this package
 
     @property
     def S(self):
@@ -133,12 +175,15 @@ class TableSpec:
         pos = np.concatenate([np.asarray(net.acceptors, np.float64).reshape(-1, 3),
                               np.asarray(net.electrodes, np.float64)[:, :3]], axis=0)
         return cls(net.N, net.P, float(net.nu), float(net.I_0), float(net.R), net.distances,
-                   net.transitions_constant, pos, float(net.ab))
+                   net.transitions_constant, pos, float(net.ab),
+                   from_positions=bool(getattr(net, "tables_from_positions", True)))
 
     def check_positions(self, rtol=1e-9):
         """True when the tables are those of the positions."""
         if self.positions is None or self.ab is None:
             return False
+        if self.from_positions:
+            return True
         from . import geometry as geo
         d = geo.site_distances(self.positions[: self.N], np.concatenate(
             [self.positions[self.N:], np.zeros((self.P, 1))], axis=1))
@@ -209,13 +254,14 @@ class TableSet:
             raise ValueError("pair_mode must be 'table' or 'positions'")
         tab_off = np.zeros(len(self.specs), np.int64)
         off = 0
+        build = pair_mode == "table"          # positions mode never reads the pair tables
         for i, t in enumerate(self.specs):
             tab_off[i] = off
-            off += 2 * t.S * t.S
+            off += 2 * t.S * t.S if build else 0
         self.tab_LB = torch.empty(max(off, 2), dtype=torch.float32, device=d)
         L = lib()
         sh = _stream_handle()
-        for i, t in enumerate(self.specs):
+        for i, t in enumerate(self.specs if build else []):
             dd = _dev(np.asarray(t.distances, np.float64).reshape(t.S, t.S), torch.float64, d)
             tc = _dev(np.asarray(t.transitions_constant, np.float64).reshape(t.S, t.S), torch.float64, d)
             check(L.kmc_build_table(t.N, t.P, float(t.nu), float(t.I_0), float(t.R), _ptr(dd), _ptr(tc),
@@ -394,18 +440,20 @@ class Batch:
                                                     self.tab_coef.data_ptr())
         return b
 
-    def launch(self, max_hops_per_launch=None, stream=None):
-        """One launch per size bin (same stream): advance every chain by up
-        to max_hops_per_launch hops (a multiple of the re-anchor period)."""
+    def launch(self, max_hops_per_launch=None, stream=None, bin_streams=None):
+        """One launch per size bin: advance every chain by up to
+        max_hops_per_launch hops (a multiple of the re-anchor period).  Bins
+        go to `stream`, or round-robin to `bin_streams` so that launches of
+        different sizes run side by side (the caller synchronises)."""
         seg = max_hops_per_launch
         if seg is None:
             seg = int(self.hops_total.max().item()) if self.n else 1
         seg = max(self.reanchor, ((int(seg) + self.reanchor - 1) // self.reanchor) * self.reanchor)
         L = lib()
-        sh = _stream_handle(stream)
-        for bin_ in self._bins:
+        for i, bin_ in enumerate(self._bins):
+            st = bin_streams[i % len(bin_streams)] if bin_streams else stream
             b = self._struct(bin_, seg)
-            check(L.kmc_run_batch(C.byref(b), sh))
+            check(L.kmc_run_batch(C.byref(b), _stream_handle(st)))
         return self
 
     def run(self, stream=None):
@@ -527,8 +575,14 @@ def simulate_go(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation, dis
     every acceptor empty (simulationWrapper.go:134-141), the caller's
     occupation comes back unchanged (pythonBind.py:84), record counts net
     traffic and credits occupancy before each hop (simulation.go:309-317).
-    Returns (time, occupation, electrode_occupation[, traffic,
-    average_occupation])."""
+    ``goSpecificFunction="wrapperSimulateProbability"`` runs the mean-field
+    relaxation instead (``meanfield.simulate_probability``).  Returns (time,
+    occupation, electrode_occupation[, traffic, average_occupation])."""
+    if goSpecificFunction == "wrapperSimulateProbability":
+        from .meanfield import simulate_probability
+        return simulate_probability(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation,
+                                    distances, E_constant, site_energies, transitions_constant,
+                                    hops=hops, record=record)
     N, P = int(N_acceptors), int(N_electrodes)
     if seed is None:
         seed = int(np.random.randint(0, 2**63 - 1, dtype=np.int64))

@@ -26,8 +26,8 @@ import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-__all__ = ["BasisFields", "boundary_owner", "solve_basis_fields", "interpolate_p1",
-           "default_cells"]
+__all__ = ["BasisFields", "boundary_owner", "solve_basis_fields", "solve_basis_fields_gpu",
+           "interpolate_p1", "default_cells", "boundary_grids"]
 
 
 def default_cells(length: float, res: float) -> int:
@@ -205,3 +205,45 @@ def interpolate_p1(field, basis: BasisFields, pts, diagonal="right"):
     v_lo = f00 + xi * (f10 - f00) + eta * (f01 - f00)
     v_up = f11 + (1 - xi) * (f01 - f11) + (1 - eta) * (f10 - f11)
     return np.where(lower, v_lo, v_up)
+
+
+def boundary_grids(xdim, ydim, electrodes, nx, ny, surplus=None):
+    """Nodal grids (P+1, ny+1, nx+1) carrying each basis field's boundary
+    data (electrode k at 1 in field k, the mu boundary at 1 in field P);
+    interior entries are 0."""
+    electrodes = np.asarray(electrodes, dtype=np.float64)
+    electrodes = electrodes.reshape(-1, electrodes.shape[-1] if electrodes.ndim == 2 else 2)
+    P = electrodes.shape[0]
+    hx, hy = xdim / nx, ydim / ny
+    X, Y = np.meshgrid(np.arange(nx + 1) * hx, np.arange(ny + 1) * hy)
+    on_b = np.zeros((ny + 1, nx + 1), dtype=bool)
+    on_b[0, :] = on_b[-1, :] = on_b[:, 0] = on_b[:, -1] = True
+    owner = boundary_owner(X[on_b], Y[on_b], xdim, ydim, electrodes, surplus)
+    grids = np.zeros((P + 1, ny + 1, nx + 1))
+    for k in range(P):
+        grids[k][on_b] = (owner == k).astype(np.float64)
+    grids[P][on_b] = (owner < 0).astype(np.float64)
+    return grids
+
+
+def solve_basis_fields_gpu(xdim, ydim, electrodes, nx, ny=None, surplus=None, dev=None):
+    """The basis fields of ``solve_basis_fields``, solved on the device by
+    kmc_laplace_basis (sine-transform direct solve of the same 5-point
+    system).  2D only."""
+    import ctypes as C
+    import torch
+    from ._native import lib, check
+    if ydim == 0:
+        return solve_basis_fields(xdim, ydim, electrodes, nx)
+    ny = nx if ny is None else ny
+    grids = boundary_grids(xdim, ydim, electrodes, nx, ny, surplus)
+    d = torch.device(dev if dev is not None else "cuda")
+    g = torch.as_tensor(grids, dtype=torch.float64).to(d).contiguous()
+    L = lib()
+    wsb = L.kmc_laplace_workspace_size(nx, ny, grids.shape[0])
+    ws = torch.empty(max(int(wsb), 8), dtype=torch.uint8, device=d)
+    st = C.c_void_p(torch.cuda.current_stream(d).cuda_stream)
+    check(L.kmc_laplace_basis(nx, ny, xdim / nx, ydim / ny, grids.shape[0], C.c_void_p(g.data_ptr()),
+                              C.c_void_p(ws.data_ptr()), wsb, st))
+    torch.cuda.synchronize(d)
+    return BasisFields(g.cpu().numpy(), xdim, ydim, nx, ny, 2)

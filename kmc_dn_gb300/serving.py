@@ -11,8 +11,11 @@ seed.  The server
   coordinates, Laplace basis fields sampled at the acceptors, donor terms),
   so a request only ships its voltages; the constant site energies of its
   chains are superposed on the device (``kmc_site_energies``);
-* admits requests in arrival order while their chain state fits the device
-  memory budget, and keeps that state resident until the request is done;
+* admits waiting requests, least work first (chains x hops x pairs per
+  hop), while their chain state fits the device memory budget and the
+  number of resident chains stays below what keeps the device busy without
+  time-slicing everything; admitted state stays resident until the request
+  is done;
 * runs every admitted request in quanta of hops on a pool of CUDA streams,
   so requests that arrive while others run are started at once and their
   launches overlap on the device; the request with the least remaining work
@@ -80,7 +83,8 @@ class Server:
     """
 
     def __init__(self, networks, *, quantum=4096, mem_budget=None, n_streams=8,
-                 pair_mode="positions", lanes=None, dev=None, short_hops=20000):
+                 pair_mode="positions", lanes=None, dev=None, short_hops=20000,
+                 max_active_chains=16384):
         if quantum % _REANCHOR:
             raise ValueError("quantum must be a multiple of the re-anchor period (1024)")
         d = torch.device(dev if dev is not None else "cuda")
@@ -93,6 +97,8 @@ class Server:
         free, _total = torch.cuda.mem_get_info(self.dev)
         self.mem_budget = int(mem_budget if mem_budget is not None else free // 4)
         self.mem_used = 0
+        self.max_active_chains = int(max_active_chains)
+        self.active_chains = 0
         lo, hi = torch.cuda.Stream.priority_range()
         self.hi_streams = [torch.cuda.Stream(device=self.dev, priority=hi) for _ in range(max(1, n_streams // 2))]
         self.lo_streams = [torch.cuda.Stream(device=self.dev, priority=lo) for _ in range(max(1, n_streams - n_streams // 2))]
@@ -105,8 +111,12 @@ class Server:
         self.finished = []
         self.lock = threading.Lock()
         self.cv = threading.Condition(self.lock)
+        # one thread at a time admits, launches and collects (the server
+        # thread, or the caller of run_sync / wait_idle when none runs)
+        self._drive = threading.Lock()
         self._thread = None
         self._stop = False
+        self._error = None
         self.hops_done = 0
 
     # ---------------------------------------------------------------- API
@@ -135,26 +145,53 @@ class Server:
         if self._thread is not None:
             self._thread.join()
             self._thread = None
+        self._raise_error()
 
     def wait_idle(self, timeout=None):
+        """Until every submitted request is finished (True), or `timeout`
+        seconds passed (False).  With the server thread running this only
+        waits; otherwise it drives the requests itself."""
         t0 = time.perf_counter()
         while True:
+            self._raise_error()
             with self.lock:
                 if not self.queue and not self.active:
                     return True
             if timeout is not None and time.perf_counter() - t0 > timeout:
                 return False
-            time.sleep(0.001)
+            if self._thread is not None and self._thread.is_alive():
+                time.sleep(0.0005)
+            else:
+                self._step()
+
+    def run_sync(self):
+        """Run everything queued to completion in the calling thread."""
+        torch.cuda.set_device(self.dev)
+        while True:
+            with self.lock:
+                if not self.queue and not self.active:
+                    return
+            self._step()
 
     # ----------------------------------------------------------- internals
+    def _work(self, req):
+        net = self.networks[req.geometry]
+        h = 0.9 * net.N           # typical hole count: pairs per hop ~ A(h)
+        pairs = h * (net.N - h) + h * net.P + net.P * (net.N - h)
+        return req.voltages.shape[0] * req.hops * pairs
+
     def _admit(self):
-        while self.queue:
-            req = self.queue[0]
+        if not self.queue:
+            return
+        waiting = sorted(self.queue, key=self._work)
+        for req in waiting:
             net = self.networks[req.geometry]
-            need = _request_bytes(req.voltages.shape[0], net.N, net.P)
-            if self.active and self.mem_used + need > self.mem_budget:
-                return
-            self.queue.popleft()
+            n = req.voltages.shape[0]
+            need = _request_bytes(n, net.N, net.P)
+            if self.active and (self.mem_used + need > self.mem_budget or
+                                self.active_chains + n > self.max_active_chains):
+                break
+            self.queue.remove(req)
             self._prepare(req, need)
 
     def _prepare(self, req, need):
@@ -172,6 +209,7 @@ class Server:
                               el_energy_dev=ve, pair_mode=self.pair_mode)
         req.bytes = need
         self.mem_used += need
+        self.active_chains += n
         self.active.append(req)
 
     def _launch_ready(self):
@@ -203,6 +241,7 @@ class Server:
                 out = dict(currents=cur, time=r["time"], electrode_occupation=np.array(r["electrode_occupation"]),
                            status=r["status"], latency=req.done_at - req.arrival)
                 self.mem_used -= req.bytes
+                self.active_chains -= req.voltages.shape[0]
                 req.batch = None
                 self.finished.append(req)
                 req.future.set_result(out)
@@ -210,29 +249,38 @@ class Server:
                 still.append(req)
         self.active = still
 
-    def _loop(self):
-        torch.cuda.set_device(self.dev)
-        while True:
-            with self.cv:
-                while not self._stop and not self.queue and not self.active:
-                    self.cv.wait(0.05)
-                if self._stop and not self.queue and not self.active:
-                    return
-                self._admit()
-            self._launch_ready()
-            self._collect()
-            time.sleep(0)
-
-    def run_sync(self):
-        """Run everything queued to completion in the calling thread."""
-        torch.cuda.set_device(self.dev)
-        while True:
+    def _step(self):
+        with self._drive:
             with self.lock:
                 self._admit()
-                if not self.queue and not self.active:
-                    return
             self._launch_ready()
             self._collect()
+
+    def _raise_error(self):
+        if self._error is not None:
+            raise RuntimeError("serving loop failed") from self._error
+
+    def _loop(self):
+        try:
+            torch.cuda.set_device(self.dev)
+            while True:
+                with self.cv:
+                    while not self._stop and not self.queue and not self.active:
+                        self.cv.wait(0.05)
+                    if self._stop and not self.queue and not self.active:
+                        return
+                self._step()
+                time.sleep(0)
+        except BaseException as e:      # fail the waiting callers instead of leaving them waiting
+            self._error = e
+            with self.lock:
+                pending = list(self.queue) + list(self.active)
+                self.queue.clear()
+                self.active = []
+            for req in pending:
+                if not req.future.done():
+                    req.future.set_exception(e)
+
 
 
 def latency_summary(requests):

@@ -30,8 +30,17 @@
  *                          Go's math/rand is replaced by a counter-based
  *                          generator (SplitMix64); results agree statistically.
  *
+ *  oracle_prob_simulate -- Go probSimulate, the mean-field relaxation of
+ *                          goSimulation/probabilitySimulation.go:53-157, FP64,
+ *                          every accumulation in the Go loop order (rates
+ *                          calcProbTransitions :7-35, step :95-110, apply
+ *                          :118-142, clamp :143-152).
+ *
  * Parity of oracle_numba_replay is pinned by tests/golden (hop sequences of
  * the reference's own function, run in plain Python with a replay stream).
+ * oracle_prob_simulate has no golden vectors (the Go toolchain is absent);
+ * it is pinned by the closed-form single-site case, where the mean-field
+ * equation is exact.
  */
 #include <math.h>
 #include <stdint.h>
@@ -289,4 +298,97 @@ int oracle_go_chains(int N, int P, double nu, double kT, double I0, double R,
     }
     free(occ);
     return 0;
+}
+
+
+/* ----------------------------------------------------------------------- */
+/* Go mean-field restatement                                                 */
+/* ----------------------------------------------------------------------- */
+
+/* probSimulate, goSimulation/probabilitySimulation.go:53-157.  occupation
+ * (N, in/out, probabilities), electrode_occupation (P, out: integrated net
+ * flow into each electrode), site_energies (N, out), traffic (S*S) and
+ * average_occupation (N) accumulated when record != 0.  Returns the
+ * simulated time, or -1 on bad arguments / allocation failure. */
+double oracle_prob_simulate(int N, int P, double nu, double kT, double I_0, double R,
+                            double *occupation, const double *distances, const double *E_constant,
+                            const double *tc, double *electrode_occupation, double *site_energies,
+                            int hops, int record, double *traffic, double *average_occupation)
+{
+    if (N < 0 || P < 0 || N + P < 1 || hops < 0) return -1.0;
+    const int S = N + P;
+    double *t = (double *)malloc(sizeof(double) * (size_t)S * S);
+    double *difference = (double *)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+    if (!t || !difference) { free(t); free(difference); return -1.0; }
+    for (int e = 0; e < P; ++e) electrode_occupation[e] = 0.0;
+    double time = 0.0;
+    for (int hop = 0; hop < hops; ++hop) {
+        /* site energies from the occupation probabilities (:85-94); the
+         * electrode entries site_energies[N..S) are the voltages */
+        for (int i = 0; i < N; ++i) {
+            difference[i] = 0.0;
+            double acc = 0.0;
+            for (int j = 0; j < N; ++j)
+                if (j != i) acc += (1.0 - occupation[j]) / distances[i * S + j];
+            site_energies[i] = E_constant[i] - I_0 * R * acc;
+        }
+        /* expected rates, their total and the net flow per site, row-major
+         * (calcProbTransitions :7-35, probTransitionPossible :37-49) */
+        double tot = 0.0;
+        for (int i = 0; i < S; ++i) {
+            for (int j = 0; j < S; ++j) {
+                double base;
+                if (i >= N && j >= N) base = 0.0;
+                else if (i >= N) base = 1.0 - occupation[j];
+                else if (j >= N) base = occupation[i];
+                else base = (1.0 - occupation[j]) * occupation[i];
+                double dE;
+                if (i < N && j < N) dE = site_energies[j] - site_energies[i] - I_0 * R / distances[i * S + j];
+                else dE = site_energies[j] - site_energies[i];
+                double r = dE > 0 ? base * nu * exp(-dE / kT) : base * nu;
+                r *= tc[i * S + j];
+                t[i * S + j] = r;
+                tot += r;
+                if (i < N) difference[i] -= r;
+                if (j < N) difference[j] += r;
+            }
+        }
+        /* largest step that keeps every probability in [0, 1] (:95-110) */
+        double max_change = 1.0;
+        for (int i = 0; i < N; ++i) {
+            const double nv = occupation[i] + difference[i] / tot;
+            if (nv < 0) {
+                const double req = occupation[i] / -(difference[i] / tot);
+                if (req < max_change) max_change = req;
+            }
+            if (nv > 1) {
+                const double req = (1.0 - occupation[i]) / (difference[i] / tot);
+                if (req < max_change) max_change = req;
+            }
+        }
+        const double time_step = 0.98 * max_change / tot;
+        time += time_step;
+        if (record)
+            for (int i = 0; i < N; ++i) average_occupation[i] += occupation[i] * time_step;
+        /* move the expected charge (:118-142) */
+        for (int i = 0; i < S; ++i) {
+            for (int j = 0; j < S; ++j) {
+                if (i >= N && j >= N) break;
+                const double rate = t[i * S + j] * max_change / tot;
+                if (i < N) occupation[i] -= rate; else electrode_occupation[i - N] -= rate;
+                if (j < N) occupation[j] += rate; else electrode_occupation[j - N] += rate;
+                if (record) {
+                    traffic[i * S + j] += rate;
+                    traffic[j * S + i] -= rate;
+                }
+            }
+        }
+        /* clamp (:143-152) */
+        for (int i = 0; i < N; ++i) {
+            if (occupation[i] < 0) occupation[i] = 0;
+            if (occupation[i] > 1) occupation[i] = 1;
+        }
+    }
+    free(t); free(difference);
+    return time;
 }

@@ -43,6 +43,10 @@ def lib():
         L.oracle_go_chains.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                        C.c_double, _u8p, _dp, _dp, _dp, _dp, C.c_int64, C.c_int64,
                                        C.c_int64, C.c_uint64, _dp, _dp, _i64p]
+        L.oracle_prob_simulate.restype = C.c_double
+        L.oracle_prob_simulate.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int,
+                                           _dp, _dp]
         _LIB = L
     return _LIB
 
@@ -100,6 +104,27 @@ def go_simulate(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_en
         int(record), _p(traffic, _dp), _p(avg, _dp), C.c_uint64(seed & (2**64 - 1)), C.byref(na))
     return dict(time=t, occupation=occ, electrode_occupation=eo, traffic=traffic,
                 average_occupation=avg[:N], n_allowed=na.value)
+
+
+def prob_simulate(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
+                  transitions_constant, hops, record=False):
+    """FP64 restatement of Go probSimulate (mean-field relaxation) for one
+    network; ``occupation`` (N probabilities) is the starting point (the Go
+    wrapper passes 0.5 everywhere).  ``site_energies`` has S entries, the
+    electrode ones being the voltages."""
+    S = N + P
+    occ = np.array(occupation, dtype=np.float64, copy=True)
+    se = np.array(site_energies, dtype=np.float64, copy=True)
+    eo = np.zeros(max(P, 1))
+    traffic = np.zeros((S, S))
+    avg = np.zeros(max(N, 1))
+    t = lib().oracle_prob_simulate(
+        N, P, nu, kT, I_0, R, _p(occ, _dp), _p(np.ascontiguousarray(distances, np.float64), _dp),
+        _p(np.ascontiguousarray(E_constant, np.float64), _dp),
+        _p(np.ascontiguousarray(transitions_constant, np.float64), _dp), _p(eo, _dp), _p(se, _dp),
+        int(hops), int(record), _p(traffic, _dp), _p(avg, _dp))
+    return dict(time=t, occupation=occ, electrode_occupation=eo[:P], site_energies=se,
+                traffic=traffic, average_occupation=avg[:N])
 
 
 def go_chains(N, P, nu, kT, I_0, R, occupations, distances, E_constant_rows, site_energy_rows,
@@ -172,3 +197,89 @@ def numba_replay_py(N, P, nu, kT, I_0, R, occupation, distances, E_constant, sit
             occ[to] = True
         log.append((fr, to))
     return np.array(log, np.int32), t
+
+
+def prob_simulate_py(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
+                     transitions_constant, hops, record=False):
+    """Plain-Python restatement of Go probSimulate (probabilitySimulation.go:
+    53-157), loop for loop; small cases only.  Cross-checks the C oracle."""
+    import math
+    S = N + P
+    occ = [float(x) for x in occupation]
+    se = [float(x) for x in site_energies]
+    d = np.asarray(distances, np.float64).reshape(S, S).tolist()
+    tc = np.asarray(transitions_constant, np.float64).reshape(S, S).tolist()
+    Ec = [float(x) for x in E_constant]
+    eo = [0.0] * P
+    traffic = [0.0] * (S * S)
+    avg = [0.0] * N
+    t = [[0.0] * S for _ in range(S)]
+    time = 0.0
+    for _ in range(int(hops)):
+        diff = [0.0] * N
+        for i in range(N):
+            acc = 0.0
+            for j in range(N):
+                if j != i:
+                    acc += (1 - occ[j]) / d[i][j]
+            se[i] = Ec[i] - I_0 * R * acc
+        tot = 0.0
+        for i in range(S):
+            for j in range(S):
+                if i >= N and j >= N:
+                    base = 0.0
+                elif i >= N:
+                    base = 1 - occ[j]
+                elif j >= N:
+                    base = occ[i]
+                else:
+                    base = (1 - occ[j]) * occ[i]
+                if i < N and j < N:
+                    dE = se[j] - se[i] - I_0 * R / d[i][j] if d[i][j] != 0 else -math.inf
+                else:
+                    dE = se[j] - se[i]
+                r = base * nu * math.exp(-dE / kT) if dE > 0 else base * nu
+                r *= tc[i][j]
+                t[i][j] = r
+                tot += r
+                if i < N:
+                    diff[i] -= r
+                if j < N:
+                    diff[j] += r
+        mc = 1.0
+        for i in range(N):
+            nv = occ[i] + diff[i] / tot
+            if nv < 0:
+                req = occ[i] / -(diff[i] / tot)
+                if req < mc:
+                    mc = req
+            if nv > 1:
+                req = (1 - occ[i]) / (diff[i] / tot)
+                if req < mc:
+                    mc = req
+        step = 0.98 * mc / tot
+        time += step
+        if record:
+            for i in range(N):
+                avg[i] += occ[i] * step
+        for i in range(S):
+            for j in range(S):
+                if i >= N and j >= N:
+                    break
+                rate = t[i][j] * mc / tot
+                if i < N:
+                    occ[i] -= rate
+                else:
+                    eo[i - N] -= rate
+                if j < N:
+                    occ[j] += rate
+                else:
+                    eo[j - N] += rate
+                if record:
+                    traffic[i * S + j] += rate
+                    traffic[j * S + i] -= rate
+        for i in range(N):
+            occ[i] = min(max(occ[i], 0.0), 1.0) if not (occ[i] != occ[i]) else occ[i]
+    return dict(time=time, occupation=np.array(occ), electrode_occupation=np.array(eo),
+                site_energies=np.array(se), traffic=np.array(traffic).reshape(S, S),
+                average_occupation=np.array(avg))

@@ -277,6 +277,7 @@ def test_positions_mode_rejects_inconsistent_tables(engine_lib):
     net = workloads.plain_network(0)
     spec = TableSpec.from_network(net)
     spec.transitions_constant = spec.transitions_constant * 1.5     # e.g. ab changed, tc not recomputed
+    spec.from_positions = False                                      # caller-supplied tables: verified
     with pytest.raises(ValueError):
         Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]],
               [net.occupation.astype(np.uint8)], [10], pair_mode="positions")

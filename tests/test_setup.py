@@ -83,3 +83,46 @@ def test_total_energy_detailed_balance():
             o2 = occ.copy(); o2[i] = False; o2[j] = True
             dE = E[j] - E[i] - IR / n.distances[i, j]
             assert abs((geo.total_energy(o2, n.distances, Ec, n.I_0, n.R) - H0) - dE) < 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_basis_fields_match_cpu_and_fenics(engine_lib):
+    """kmc_laplace_basis (sine-transform direct solve on the device) gives the
+    host FD solution, and so the reference's FEniCS potential."""
+    from kmc_dn_gb300.laplace import solve_basis_fields_gpu
+    f = load_golden(FIXTURES[0])
+    for k in range(min(3, len(f["N"]))):
+        xdim, ydim, res = float(f["xdim"][k]), float(f["ydim"][k]), float(f["res"][k])
+        el = f["electrodes"][k]
+        nx, ny = default_cells(xdim, res), default_cells(ydim, res)
+        cpu = solve_basis_fields(xdim, ydim, el[:, :2], nx, ny)
+        gpu = solve_basis_fields_gpu(xdim, ydim, el[:, :2], nx, ny)
+        np.testing.assert_allclose(gpu.fields, cpu.fields, atol=1e-11, rtol=0)
+        ev = gpu.sample(f["acceptors"][k][:, :2])
+        V = el[:, 3] @ ev[:-1] + float(f["mu"][k]) * ev[-1]
+        err = np.max(np.abs(V - f["eV_constant"][k])) / np.max(np.abs(f["eV_constant"][k]))
+        assert err < 1e-11, err
+    # a rectangular, anisotropic mesh too
+    el = np.array([[0.0, 1.0], [3.0, 1.0], [1.5, 0.0], [1.5, 2.0]])
+    cpu = solve_basis_fields(3.0, 2.0, el, 60, 45)
+    gpu = solve_basis_fields_gpu(3.0, 2.0, el, 60, 45)
+    np.testing.assert_allclose(gpu.fields, cpu.fields, atol=1e-11, rtol=0)
+
+
+@pytest.mark.gpu
+def test_gpu_p1_sampling_matches_host(engine_lib):
+    import ctypes as C
+    import torch
+    from kmc_dn_gb300._native import lib, check
+    from kmc_dn_gb300.laplace import interpolate_p1
+    el = np.array([[0.0, 5.0], [20.0, 5.0], [5.0, 0.0], [5.0, 20.0]])
+    bf = solve_basis_fields(20.0, 20.0, el, 100, 100)
+    pts = np.random.default_rng(0).uniform(0, 20, (500, 2))
+    g = torch.as_tensor(bf.fields).cuda().contiguous()
+    xy = torch.as_tensor(pts).cuda().contiguous()
+    out = torch.zeros(bf.fields.shape[0] * 500, dtype=torch.float64, device="cuda")
+    check(lib().kmc_p1_sample(100, 100, 0.2, 0.2, bf.fields.shape[0], C.c_void_p(g.data_ptr()), 500,
+                              C.c_void_p(xy.data_ptr()), C.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    host = np.stack([interpolate_p1(f, bf, pts) for f in bf.fields])
+    np.testing.assert_allclose(out.cpu().numpy().reshape(host.shape), host, rtol=1e-13, atol=1e-13)
