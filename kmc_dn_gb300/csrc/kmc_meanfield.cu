@@ -13,17 +13,19 @@
 //   apply     o_i += m (in_i - out_i) / sum t, the electrodes' counters
 //             likewise; clamp to [0, 1]                            (:118-152)
 //
-// One thread block per network; the pair tables (K = nu tc, B = I_0 R / d)
-// and the iteration's S x S rates live in shared memory, so an iteration
-// touches no global memory outside record mode.  Warp w owns rows
-// w, w + 8, ... for the energies, the rates and the row sums (outflows),
-// then columns for the inflows; every sum runs in a fixed order, so a run
-// is deterministic.  Two rate precisions:
-//   KMC_MF_RATES_F64  exp() in FP64 (the reference's arithmetic up to
-//                     rounding order),
-//   KMC_MF_RATES_F32  ex2.approx.f32 on FP32 copies of the state, sums in
-//                     FP64: GB300's FP64 pipe runs at 1/64 of FP32, so the
-//                     exponentials move to the SFU.
+// One block of 128 threads per network; the pair tables (K = nu tc,
+// B = I_0 R / d) and the iteration's S x S rates live in shared memory, so
+// an iteration touches no global memory outside record mode.  A thread per
+// acceptor sums its energy, a thread per pair evaluates a rate, a thread per
+// site sums its row (outflow) or its column (inflow) in a fixed order, so a
+// run is deterministic and a network's result does not depend on the batch.
+// Two rate precisions:
+//   KMC_MF_RATES_F64  everything in FP64, exp() per pair (the reference's
+//                     arithmetic up to rounding order),
+//   KMC_MF_RATES_F32  FP32 energies and rates (one ex2.approx per pair),
+//                     compensated FP32 row/column sums, FP64 state, step
+//                     and clock: GB300 runs FP64 at 1/64 of FP32, so only
+//                     O(S) FP64 work per iteration remains.
 // No spin-waits; every loop is bounded by the iteration count or S.
 #include <algorithm>
 #include <cmath>
@@ -35,7 +37,7 @@
 namespace kmc {
 namespace {
 
-constexpr int kMfThreads = 256;
+constexpr int kMfThreads = 128;
 constexpr int kMfWarps = kMfThreads / 32;
 constexpr int kMfSmemLimit = 226 * 1024;   // dynamic; leaves room for the static words
 
@@ -64,20 +66,48 @@ template <bool F64> struct MfTypes;
 template <> struct MfTypes<true> { using Real = double; using Pair = double2; };
 template <> struct MfTypes<false> { using Real = float; using Pair = float2; };
 
+// Running sum of one thread: plain FP64, or in FP32 as an unevaluated pair
+// (hi, lo) updated by TwoSum (Knuth), six FP32 operations per term, which
+// keeps the sum of FP32 terms to about 2^-44 relative without the FP64
+// pipe.
+template <bool F64> struct Acc;
+template <> struct Acc<true> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct Acc<false> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float t = __fadd_rn(hi, x);
+        const float bp = __fsub_rn(t, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+        hi = t;
+        lo = __fadd_rn(lo, err);
+    }
+    __device__ __forceinline__ double value() const { return static_cast<double>(hi) + static_cast<double>(lo); }
+};
+
+// Row stride of the shared S x S arrays: odd, so that a thread per row
+// reading along its row and a thread per column reading down it both hit
+// distinct banks.
+__device__ __host__ __forceinline__ int row_stride(int S) { return S | 1; }
+
 }  // namespace
 
 size_t mf_smem_bytes(int S, int rates)
 {
-    const size_t pairs = static_cast<size_t>(S) * S;
+    const size_t pairs = static_cast<size_t>(S) * row_stride(S);
     const size_t per_pair = rates == KMC_MF_RATES_F64 ? 16 + 8 : 8 + 4;
-    // occ, e, out, in, avg, eo (double) + e, occ (float) per site, + scalars
+    // occ, out, in, avg, eo (double) + e (Real) + occ, e (float) per site, + scalars
     return pairs * per_pair + static_cast<size_t>(S) * (6 * 8 + 2 * 4) + 64;
 }
 
 namespace {
 
 template <bool F64>
-__global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
+__global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batch b)
 {
     using Real = typename MfTypes<F64>::Real;
     using Pair = typename MfTypes<F64>::Pair;
@@ -86,6 +116,7 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int N = b.N[c], P = b.P[c], S = N + P;
     const int SS = S * S;
+    const int SP = row_stride(S);
     if (S < 1 || S > b.max_sites) {
         if (tid == 0 && b.status) b.status[c] = KMC_ERR_INVALID;
         return;
@@ -97,18 +128,17 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
     double *se_out = b.site_energies + b.site_off[c];
     double *occ_io = b.occupation + b.site_off[c];
 
-    // shared-memory carve (8-byte items first)
+    // shared-memory carve (8-byte items first); S x S arrays use row stride SP
     Pair *KB = reinterpret_cast<Pair *>(smem);
-    Real *rt = reinterpret_cast<Real *>(KB + SS);
+    Real *rt = reinterpret_cast<Real *>(KB + S * SP);
     double *occ = reinterpret_cast<double *>(
-        (reinterpret_cast<uintptr_t>(rt + SS) + 15) & ~static_cast<uintptr_t>(15));
-    double *e = occ + S;
-    double *outs = e + S;
+        (reinterpret_cast<uintptr_t>(rt + S * SP) + 15) & ~static_cast<uintptr_t>(15));
+    double *outs = occ + S;
     double *ins = outs + S;
     double *avg = ins + S;
     double *eo = avg + S;
-    float *ef = reinterpret_cast<float *>(eo + S);
-    float *of = ef + S;
+    Real *e = reinterpret_cast<Real *>(eo + S);   // site energies (electrodes: voltages)
+    float *of = reinterpret_cast<float *>(e + S);  // FP32 copy of the probabilities
     __shared__ double sh_tot, sh_mc, sh_time;
     __shared__ int sh_stop;
 
@@ -117,73 +147,74 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
         const int i = p / S, j = p - (p / S) * S;
         const double K = nu * tcon[p];
         const double B = (i < N && j < N) ? I0R / dist[p] : 0.0;
-        KB[p] = Pair{static_cast<Real>(K), static_cast<Real>(B)};
+        KB[i * SP + j] = Pair{static_cast<Real>(K), static_cast<Real>(B)};
     }
     for (int k = tid; k < S; k += kMfThreads) {
         occ[k] = k < N ? occ_io[k] : 0.0;
-        e[k] = k < N ? 0.0 : se_out[k];          // electrode entries: the voltages
+        of[k] = static_cast<float>(occ[k]);
+        e[k] = k < N ? Real(0) : static_cast<Real>(se_out[k]);
         avg[k] = (b.record && k < N) ? b.average_occupation[b.site_off[c] + k] : 0.0;
         eo[k] = 0.0;
     }
     if (tid == 0) { sh_time = 0.0; sh_stop = 0; }
     __syncthreads();
 
+    const Real ec_i = tid < N ? static_cast<Real>(Ec[tid]) : Real(0);
     const double inv_kT = 1.0 / kT;
     const float c2 = static_cast<float>(1.4426950408889634 / kT);
     const int64_t hops = b.hops[c];
     double *traffic = b.record ? b.traffic + b.traffic_off[c] : nullptr;
     int64_t it = 0;
     for (; it < hops; ++it) {
-        // (1) energies from the probabilities
-        for (int i = warp; i < N; i += kMfWarps) {
-            double acc = 0.0;
-            for (int j = lane; j < N; j += 32)
-                if (j != i) acc += (1.0 - occ[j]) * static_cast<double>(KB[i * S + j].y);
-            acc = warp_sum(acc);
-            if (lane == 0) e[i] = Ec[i] - acc;
-        }
-        __syncthreads();
-        if (!F64)
-            for (int k = tid; k < S; k += kMfThreads) { ef[k] = static_cast<float>(e[k]); of[k] = static_cast<float>(occ[k]); }
-        if (!F64) __syncthreads();
-
-        // (2) rates and outflows, warp per row
-        for (int i = warp; i < S; i += kMfWarps) {
-            double row = 0.0;
-            for (int j = lane; j < S; j += 32) {
-                const Pair kb = KB[i * S + j];
-                Real r;
-                if (F64) {
-                    double w;
-                    if (i >= N && j >= N) w = 0.0;
-                    else if (i >= N) w = 1.0 - occ[j];
-                    else if (j >= N) w = occ[i];
-                    else w = (1.0 - occ[j]) * occ[i];
-                    const double dE = e[j] - e[i] - static_cast<double>(kb.y);
-                    r = static_cast<Real>(w * static_cast<double>(kb.x) * exp(-fmax(dE, 0.0) * inv_kT));
-                } else {
-                    float w;
-                    if (i >= N && j >= N) w = 0.0f;
-                    else if (i >= N) w = 1.0f - of[j];
-                    else if (j >= N) w = of[i];
-                    else w = (1.0f - of[j]) * of[i];
-                    const float dE = ef[j] - ef[i] - static_cast<float>(kb.y);
-                    r = static_cast<Real>(w * static_cast<float>(kb.x) * ex2_approx(-c2 * fmaxf(dE, 0.0f)));
-                }
-                rt[i * S + j] = r;
-                row += static_cast<double>(r);
+        // (1) energies from the probabilities, a thread per acceptor
+        for (int i = tid; i < N; i += kMfThreads) {
+            Real acc = 0;
+            for (int j = 0; j < N; ++j) {
+                const Real w = F64 ? static_cast<Real>(1.0 - occ[j]) : static_cast<Real>(1.0f - of[j]);
+                if (j != i) acc += w * KB[i * SP + j].y;
             }
-            row = warp_sum(row);
-            if (lane == 0) outs[i] = row;
+            e[i] = (i == tid ? ec_i : static_cast<Real>(Ec[i])) - acc;
         }
         __syncthreads();
 
-        // (3) inflows, warp per column
-        for (int j = warp; j < S; j += kMfWarps) {
-            double col = 0.0;
-            for (int i = lane; i < S; i += 32) col += static_cast<double>(rt[i * S + j]);
-            col = warp_sum(col);
-            if (lane == 0) ins[j] = col;
+        // (2) the S x S expected rates, a thread per pair
+        for (int p = tid; p < SS; p += kMfThreads) {
+            const int i = p / S, j = p - (p / S) * S;
+            const Pair kb = KB[i * SP + j];
+            Real r;
+            if (F64) {
+                double w;
+                if (i >= N && j >= N) w = 0.0;
+                else if (i >= N) w = 1.0 - occ[j];
+                else if (j >= N) w = occ[i];
+                else w = (1.0 - occ[j]) * occ[i];
+                const double dE = static_cast<double>(e[j]) - static_cast<double>(e[i]) - static_cast<double>(kb.y);
+                r = static_cast<Real>(w * static_cast<double>(kb.x) * exp(-fmax(dE, 0.0) * inv_kT));
+            } else {
+                float w;
+                if (i >= N && j >= N) w = 0.0f;
+                else if (i >= N) w = 1.0f - of[j];
+                else if (j >= N) w = of[i];
+                else w = (1.0f - of[j]) * of[i];
+                const float dE = static_cast<float>(e[j]) - static_cast<float>(e[i]) - static_cast<float>(kb.y);
+                r = static_cast<Real>(w * static_cast<float>(kb.x) * ex2_approx(-c2 * fmaxf(dE, 0.0f)));
+            }
+            rt[i * SP + j] = r;
+        }
+        __syncthreads();
+
+        // (3) outflows (threads 0..S-1, along rows) and inflows (threads
+        // S..2S-1, down columns), each a sequential sum in a fixed order
+        for (int q = tid; q < 2 * S; q += kMfThreads) {
+            Acc<F64> a;
+            if (q < S) {
+                for (int j = 0; j < S; ++j) a.add(rt[q * SP + j]);
+                outs[q] = a.value();
+            } else {
+                const int k = q - S;
+                for (int i = 0; i < S; ++i) a.add(rt[i * SP + k]);
+                ins[k] = a.value();
+            }
         }
         __syncthreads();
 
@@ -223,6 +254,7 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
                 double o = occ[k] + net * f;
                 o = o < 0.0 ? 0.0 : (o > 1.0 ? 1.0 : o);
                 occ[k] = o;
+                of[k] = static_cast<float>(o);
             } else {
                 eo[k] += net * f;
             }
@@ -231,7 +263,7 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
             for (int p = tid; p < SS; p += kMfThreads) {
                 const int i = p / S, j = p - (p / S) * S;
                 if (i >= N && j >= N) continue;
-                traffic[p] += (static_cast<double>(rt[p]) - static_cast<double>(rt[j * S + i])) * f;
+                traffic[p] += (static_cast<double>(rt[i * SP + j]) - static_cast<double>(rt[j * SP + i])) * f;
             }
         __syncthreads();
     }
@@ -240,7 +272,7 @@ __global__ void __launch_bounds__(kMfThreads) mf_kernel(kmc_mf_batch b)
     for (int k = tid; k < S; k += kMfThreads) {
         if (k < N) {
             occ_io[k] = occ[k];
-            se_out[k] = e[k];
+            se_out[k] = static_cast<double>(e[k]);
             if (b.record) b.average_occupation[b.site_off[c] + k] = avg[k];
         } else {
             b.electrode_occupation[b.el_off[c] + (k - N)] = eo[k];

@@ -46,7 +46,7 @@ from .engine import Batch, TableSet, TableSpec, _REANCHOR, superpose
 __all__ = ["Request", "Server", "latency_summary"]
 
 
-@dataclass
+@dataclass(eq=False)          # identity: queue removal must not compare voltage arrays
 class Request:
     geometry: int
     voltages: np.ndarray            # (C, P)

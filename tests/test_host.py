@@ -41,3 +41,15 @@ def test_native_library_missing_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(_native, "_LIB", None)
     with pytest.raises(_native.NativeLibraryError):
         _native.lib()
+
+
+def test_serving_queue_removes_requests_by_identity():
+    """Requests carry voltage arrays; removing one from the wait queue must
+    not compare arrays (that raised inside the server thread)."""
+    from collections import deque
+    from kmc_dn_gb300.serving import Request
+    a = Request(0, np.zeros((3, 8)), 10, 1, arrival=0.0)
+    b = Request(0, np.zeros((5, 8)), 10, 2, arrival=0.0)
+    q = deque([a, b])
+    q.remove(b)
+    assert list(q) == [a] and a != Request(0, np.zeros((3, 8)), 10, 1, arrival=0.0)
