@@ -220,7 +220,7 @@ def main():
     ap.add_argument("--hops", type=int, default=HOPS)
     ap.add_argument("--chains", type=int, default=N_CHAINS)
     ap.add_argument("--lanes", type=int, default=0)
-    ap.add_argument("--warps-per-block", type=int, default=4)
+    ap.add_argument("--warps-per-block", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
@@ -331,13 +331,17 @@ def main():
     peak = C.c_double(0)
     _native.check(_native.lib().kmc_measure_ex2_rate(C.byref(peak)))
     achieved = pairs_per_step / (ms_per_step * 1e-3)
+    # DRAM bytes of one engine launch from the committed ncu summary (the
+    # kernel's traffic is the one-time state load: it does not grow with hops)
     traffic = None
-    tpath = os.path.join(HERE, "profiles", "engine_traffic.json")
+    tpath = os.path.join(HERE, "profiles", "warp_engine_homogeneous.md")
     if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
-        except (ValueError, OSError):
-            traffic = None
+        for line in open(tpath):
+            if line.startswith("DRAM bytes per launch (read + write):"):
+                try:
+                    traffic = int(line.split(":")[1].strip())
+                except ValueError:
+                    traffic = None
 
     out = None
     if rank == 0:
@@ -625,7 +629,7 @@ def bench_serving(args):
     from kmc_dn_gb300 import workloads
     from kmc_dn_gb300.serving import Server, latency_summary
     nets = workloads.serving_geometries(seed=args.seed)
-    srv = Server(nets, quantum=4096, n_streams=8)
+    srv = Server(nets, quantum=20480)
     rng = np.random.Generator(np.random.PCG64(args.seed + 77))
     n_req = rng.poisson(args.rate * args.serve_seconds)
     gaps = rng.exponential(1.0 / args.rate, n_req)
@@ -651,14 +655,19 @@ def bench_serving(args):
     srv.stop(drain=False)
     done = [r for r in submitted if r.done_at is not None]
     lat = latency_summary(done)
+    for gi, net in enumerate(nets):
+        sub = [r for r in done if r.geometry == gi]
+        if sub:
+            lat[f"N{net.N}"] = latency_summary(sub)
     return {"metric": METRIC, "value": srv.hops_done / wall, "unit": "hops/s", "n_gpus": 1, "steps": 1,
             "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "serving: Poisson voltage-search requests on 4 resident geometries",
                        "rate_per_s": args.rate, "arrival_window_s": args.serve_seconds,
                        "requests": int(n_req), "completed": len(done), "drained": bool(drained),
-                       "quantum_hops": 4096},
-            "latency": lat, "gpu_launches": None}
+                       "quantum_hops": srv.quantum, "quantum_long_hops": srv.quantum_long,
+                       "max_active_long_chains": srv.max_active_long_chains},
+            "latency": lat, "gpu_launches": srv.launches}
 
 
 if __name__ == "__main__":

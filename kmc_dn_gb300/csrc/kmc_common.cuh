@@ -32,10 +32,11 @@ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1
     return c;
 }
 
-// Uniform in (0,1) from 32 bits: (x + 1/2) * 2^-32 (never 0, never 1).
+// Uniform in (0,1) from the top 23 bits: (k + 1/2) 2^-23, exact in FP32,
+// so never 0 and at most 1 - 2^-24.
 __device__ __forceinline__ float u01_from32(uint32_t x)
 {
-    return (static_cast<float>(x >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    return (static_cast<float>(x >> 9) + 0.5f) * (1.0f / 8388608.0f);
 }
 
 // Uniform in (0,1) with 53 random bits from two words.
@@ -43,16 +44,6 @@ __device__ __forceinline__ double u01_from64(uint32_t hi, uint32_t lo)
 {
     const uint64_t v = ((static_cast<uint64_t>(hi) << 32) | lo) >> 11;
     return (static_cast<double>(v) + 0.5) * 0x1.0p-53;
-}
-
-// Uniform in (0,1) from 52 random bits with one FP64 operation: the bits
-// fill the mantissa of a double in [1,2) whose lowest bit is forced to 1
-// (so the result is never 0; it is at most 1 - 2^-52), and 1 is subtracted.
-__device__ __forceinline__ double u01_from52(uint32_t hi, uint32_t lo)
-{
-    const double one_two = __hiloint2double(static_cast<int>(0x3FF00000u | (hi >> 12)),
-                                            static_cast<int>(lo | 1u));
-    return one_two - 1.0;
 }
 
 // ---------------------------------------------------------------------------

@@ -22,12 +22,14 @@
 //               passes, shared by the chains of one geometry) or, in
 //               positions mode, from the sites' coordinates carried in the
 //               lists (d from one rsqrt; no table traffic).
-//  selection    The per-thread sums are scanned in FP64; the clock advances
-//               by Exp(1)/total accumulated in FP64 (simulation.go:297-298);
-//               the event is the first pair whose cumulative rate reaches
-//               u*total (kmc_dopant_networks.py:106-110): the FP64 compare
-//               picks the thread, then that thread's run is re-evaluated by
-//               the group and scanned relative to its FP64 base.
+//  selection    The per-thread sums are scanned in double-float (two FP32
+//               words, about 47 bits; GB300's FP64 rate is 1/64 of FP32);
+//               the clock advances by Exp(1)/total, accumulated the same way
+//               (simulation.go:297-298); the event is the first pair whose
+//               cumulative rate reaches u*total (kmc_dopant_networks.py:
+//               106-110), u with 47 random bits: the double-float compare
+//               picks the thread, then that thread's stored running sums
+//               (or its re-evaluated run) are searched relative to its base.
 //  hop          O(N) incremental energy update (makeJump,
 //               simulation.go:107-130), occupancy bits, electrode counters,
 //               optional record (numba or Go convention); every `reanchor`
@@ -71,6 +73,63 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: a value hi + lo held in two floats.  GB300 issues
+// FP64 at 1/64 of the FP32 rate, so the per-hop scan, event target and clock
+// run in this form; TwoSum / TwoProduct (Knuth, Dekker) keep them exact to
+// about 2^-47 relative.
+// ---------------------------------------------------------------------------
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+    return F2{s, e};
+}
+
+// (x + y), normalised so that |lo| <= ulp(hi) / 2
+__device__ __forceinline__ F2 df_add(F2 x, F2 y)
+{
+    const F2 s = two_sum(x.hi, y.hi);
+    const float lo = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+    const float hi = __fadd_rn(s.hi, lo);
+    return F2{hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+
+__device__ __forceinline__ F2 df_mul(F2 x, F2 y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);          // exact error of the product
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    const float hi = __fadd_rn(p, e);
+    return F2{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+// x >= y for normalised values
+__device__ __forceinline__ bool df_ge(F2 x, F2 y) { return x.hi > y.hi || (x.hi == y.hi && x.lo >= y.lo); }
+
+__device__ __forceinline__ double df_to_double(F2 x) { return static_cast<double>(x.hi) + static_cast<double>(x.lo); }
+
+__device__ __forceinline__ F2 df_from_double(double v)
+{
+    const float hi = static_cast<float>(v);
+    return F2{hi, static_cast<float>(v - static_cast<double>(hi))};
+}
+
+// Uniform in (0,1) with 47 random bits, (A + 1/2) 2^-47, as hi + lo.
+__device__ __forceinline__ F2 u01_df(uint32_t a, uint32_t b)
+{
+    const uint64_t A = ((static_cast<uint64_t>(a) << 15) | (b >> 17)) & ((1ull << 47) - 1);
+    const float hi = static_cast<float>(static_cast<uint32_t>(A >> 23)) * (1.0f / 16777216.0f);
+    const float lo = (static_cast<float>(static_cast<uint32_t>(A & 0x7fffffu)) + 0.5f) * 0x1.0p-47f;
+    return F2{hi, lo};
 }
 
 // k -> (row, col) within the pair enumeration.  Float-reciprocal quotient
@@ -183,20 +242,6 @@ struct WarpGroup {
         mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (sub * G);
     }
     __device__ __forceinline__ void sync() const { __syncwarp(mask); }
-    // inclusive FP64 scan; sets the exclusive value and the total
-    __device__ __forceinline__ double scan(double v, double &excl, double &tot) const
-    {
-        double x = v;
-#pragma unroll
-        for (int d = 1; d < G; d <<= 1) {
-            const double o = __shfl_up_sync(mask, x, d, G);
-            if (g >= d) x += o;
-        }
-        const double e = __shfl_up_sync(mask, x, 1, G);
-        excl = g == 0 ? 0.0 : e;
-        tot = __shfl_sync(mask, x, G - 1, G);
-        return x;
-    }
     __device__ __forceinline__ float scanf(float v, float &tot) const
     {
         float x = v;
@@ -223,6 +268,25 @@ struct WarpGroup {
     }
     template <typename V>
     __device__ __forceinline__ V bcast(V v, int src) const { return __shfl_sync(mask, v, src, G); }
+    __device__ __forceinline__ F2 bcast2(F2 v, int src) const
+    {
+        return F2{__shfl_sync(mask, v.hi, src, G), __shfl_sync(mask, v.lo, src, G)};
+    }
+    // inclusive double-float scan of FP32 values; sets the exclusive value
+    // and the total
+    __device__ __forceinline__ F2 scan_df(float v, F2 &excl, F2 &tot) const
+    {
+        F2 x{v, 0.0f};
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const F2 o{__shfl_up_sync(mask, x.hi, d, G), __shfl_up_sync(mask, x.lo, d, G)};
+            if (g >= d) x = df_add(x, o);
+        }
+        const F2 e{__shfl_up_sync(mask, x.hi, 1, G), __shfl_up_sync(mask, x.lo, 1, G)};
+        excl = g == 0 ? F2{0.0f, 0.0f} : e;
+        tot = bcast2(x, G - 1);
+        return x;
+    }
 };
 
 // Block-wide group; its scratch lives in static shared memory.
@@ -235,35 +299,6 @@ struct BlockGroup {
     int *si;      // [2]
     __device__ __forceinline__ void init() { g = threadIdx.x; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
-    __device__ double scan(double v, double &excl, double &tot) const
-    {
-        const int lane = g & 31, w = g >> 5;
-        double x = v;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const double o = __shfl_up_sync(0xffffffffu, x, d);
-            if (lane >= d) x += o;
-        }
-        if (lane == 31) sd[w] = x;
-        __syncthreads();
-        if (w == 0) {
-            double y = lane < kWarps ? sd[lane] : 0.0;
-#pragma unroll
-            for (int d = 1; d < kWarps; d <<= 1) {
-                const double o = __shfl_up_sync(0xffffffffu, y, d);
-                if (lane >= d) y += o;
-            }
-            if (lane < kWarps) sd[lane] = y;
-        }
-        __syncthreads();
-        const double base = w > 0 ? sd[w - 1] : 0.0;
-        tot = sd[kWarps - 1];
-        __syncthreads();
-        x += base;
-        const double prev = __shfl_up_sync(0xffffffffu, x, 1);
-        excl = lane > 0 ? prev : base;
-        return x;
-    }
     __device__ float scanf(float v, float &tot) const
     {
         const int lane = g & 31, w = g >> 5;
@@ -311,6 +346,37 @@ struct BlockGroup {
         __syncthreads();
         return r;
     }
+    __device__ F2 scan_df(float v, F2 &excl, F2 &tot) const
+    {
+        const int lane = g & 31, w = g >> 5;
+        F2 x{v, 0.0f};
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const F2 o{__shfl_up_sync(0xffffffffu, x.hi, d), __shfl_up_sync(0xffffffffu, x.lo, d)};
+            if (lane >= d) x = df_add(x, o);
+        }
+        F2 *s2 = reinterpret_cast<F2 *>(sd);      // kWarps slots of 8 bytes
+        if (lane == 31) s2[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            F2 y = lane < kWarps ? s2[lane] : F2{0.0f, 0.0f};
+#pragma unroll
+            for (int d = 1; d < kWarps; d <<= 1) {
+                const F2 o{__shfl_up_sync(0xffffffffu, y.hi, d), __shfl_up_sync(0xffffffffu, y.lo, d)};
+                if (lane >= d) y = df_add(y, o);
+            }
+            if (lane < kWarps) s2[lane] = y;
+        }
+        __syncthreads();
+        const F2 base = w > 0 ? s2[w - 1] : F2{0.0f, 0.0f};
+        tot = s2[kWarps - 1];
+        __syncthreads();
+        x = df_add(x, base);
+        const F2 prev{__shfl_up_sync(0xffffffffu, x.hi, 1), __shfl_up_sync(0xffffffffu, x.lo, 1)};
+        excl = lane > 0 ? prev : base;
+        return x;
+    }
+    __device__ F2 bcast2(F2 v, int src) const { return bcast(v, src); }
     template <typename V>
     __device__ V bcast(V v, int src) const
     {
@@ -423,7 +489,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     int h = 0;
     for (int w = 0; w < W; ++w) h += __popc(sm.occw[w]);
 
-    double t = B.time[c];
+    F2 t = df_from_double(B.time[c]);    // the clock, double-float
     int64_t hop = hops_done0;
     const int64_t hop_end = hops_done0 + (todo > 0 ? todo : 0);
     int status = KMC_OK;
@@ -433,7 +499,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     double *occ_since = record ? B.occ_since + so : nullptr;
     int32_t *traffic = record ? B.traffic + B.chain_pair_off[c] : nullptr;
     if (record)
-        for (int j = g; j < N; j += G) occ_since[j] = t;
+        for (int j = g; j < N; j += G) occ_since[j] = df_to_double(t);
 
     // Energies from scratch (E_j = Ec_j - sum_{k empty} B_jk) and the ordered
     // lists built from them.  Run at the launch start and at every absolute
@@ -479,7 +545,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // Thread g holds the two uniforms of hop rbase + (g mod 32), already
     // mapped: the clock's Exp(1) variate and the event uniform.
     float rnd_e1 = 0.0f;
-    double rnd_u = 0.0;
+    F2 rnd_u{0.0f, 0.0f};
     int64_t rbase = INT64_MIN / 2;
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
 
@@ -553,11 +619,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         npairs += static_cast<unsigned long long>(A);
         // ---- uniforms for this hop ----
-        double u_ev;
+        F2 u_ev;
         float e1;
         if (replay) {
             e1 = -log1pf(-static_cast<float>(replay[2 * hop]));
-            u_ev = replay[2 * hop + 1];
+            u_ev = df_from_double(replay[2 * hop + 1]);
         } else {
             if (hop - rbase >= RW) {
                 rbase = hop;
@@ -567,22 +633,22 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                                                     static_cast<uint32_t>(stream >> 32)},
                                               k0, k1);
                 rnd_e1 = -__logf(u01_from32(w.x));
-                rnd_u = u01_from52(w.y, w.z);
+                rnd_u = u01_df(w.y, w.z);
             }
             const int ri = static_cast<int>(hop - rbase);
             e1 = grp.bcast(rnd_e1, ri);
-            u_ev = grp.bcast(rnd_u, ri);
+            u_ev = grp.bcast2(rnd_u, ri);
         }
         if (sm.rates) grp.sync();   // stored rates visible to the whole group
         // ---- FP64 scan of the per-thread sums ----
-        double excl, tot;
-        const double incl = grp.scan(static_cast<double>(lsum), excl, tot);
-        if (!(tot > 0.0) || !(tot < 1.0e300)) { status = KMC_ERR_NONFINITE; break; }
-        const double target = u_ev * tot;
-        int L = grp.first(incl >= target);
+        F2 excl, tot;
+        const F2 incl = grp.scan_df(lsum, excl, tot);
+        if (!(tot.hi > 0.0f) || !(tot.hi <= 3.0e38f)) { status = KMC_ERR_NONFINITE; break; }
+        const F2 target = df_mul(u_ev, tot);
+        int L = grp.first(df_ge(incl, target));
         if (L < 0) L = G - 1;
-        const double baseL = grp.bcast(excl, L);
-        float rem = static_cast<float>(target - baseL);
+        const F2 baseL = grp.bcast2(excl, L);
+        float rem = df_add(target, F2{-baseL.hi, -baseL.lo}).hi;
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
@@ -637,9 +703,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const int from = Pairs::kSiteInRec ? Pairs::site(sm.src[row]) : sm.src_id[row];
         const int to = Pairs::kSiteInRec ? Pairs::site(sm.tgt[col]) : sm.tgt_id[col];
         // ---- clock ----
-        const float dt = e1 * __frcp_rn(static_cast<float>(tot));
-        const double t_before = t;
-        t += static_cast<double>(dt);
+        const float dt = e1 * __frcp_rn(tot.hi);
+        const F2 t_before = t;
+        t = df_add(t, F2{dt, 0.0f});
         grp.sync();   // every thread is done reading the lists and rates
         // ---- apply the hop and rebuild the lists in one pass ----
         const bool fa = from < N, tb = to < N;
@@ -687,7 +753,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             if (record) {
                 traffic[from * S + to] += 1;
                 if (record == KMC_RECORD_GO) traffic[to * S + from] -= 1;
-                const double tx = (record == KMC_RECORD_GO) ? t : t_before;
+                const double tx = df_to_double((record == KMC_RECORD_GO) ? t : t_before);
                 if (fa) occ_time[from] += tx - occ_since[from];
                 if (tb) occ_since[to] = tx;
             }
@@ -699,16 +765,17 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 
     // ---- write back ----
     if (record) {
+        const double td = df_to_double(t);
         for (int j = g; j < N; j += G)
             if ((sm.occw[j >> 5] >> (j & 31)) & 1u) {
-                occ_time[j] += t - occ_since[j];
-                occ_since[j] = t;
+                occ_time[j] += td - occ_since[j];
+                occ_since[j] = td;
             }
     }
     for (int j = g; j < N; j += G) occ_g[j] = static_cast<uint8_t>((sm.occw[j >> 5] >> (j & 31)) & 1u);
     for (int e = g; e < P; e += G) B.electrode_occupation[eoff + e] += sm.eo[e];
     if (g == 0) {
-        B.time[c] = t;
+        B.time[c] = df_to_double(t);
         B.hops_done[c] = hop;
         B.status[c] = status;
         if (B.n_pairs) B.n_pairs[c] += npairs;
@@ -734,8 +801,11 @@ __device__ __forceinline__ const float2 *stage_table(const kmc_batch &B, uint32_
 // bound of 3 blocks of 256 threads keeps registers at or below 85 so that
 // 24 warps fit on an SM.  table_words > 0: every chain of the launch uses
 // table 0, staged in shared memory ahead of the per-chain areas.
+#ifndef KMC_WARP_MIN_BLOCKS
+#define KMC_WARP_MIN_BLOCKS 3
+#endif
 template <int G, typename Pairs>
-__global__ void __launch_bounds__(256, 3) warp_engine_kernel(const kmc_batch B, int rate_words,
+__global__ void __launch_bounds__(256, KMC_WARP_MIN_BLOCKS) warp_engine_kernel(const kmc_batch B, int rate_words,
                                                              int table_words)
 {
     constexpr int CPW = 32 / G;
@@ -809,6 +879,10 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
     const int wpb = b.warps_per_block;
     const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
     int rw = rate_buffer_words(b.max_sites, G);
+    // Pad each chain's area to G words modulo 32: the 32/G chains of a warp
+    // then store their running sums (element i of thread g at i*G + g) to
+    // disjoint banks.
+    if (G < 32) rw += ((G - (lw + rw)) % 32 + 32) % 32;
     if (static_cast<size_t>(wpb) * CPW * (lw + rw) * 4 > kSmemBudget) rw = 0;   // recompute instead
     const size_t chains = static_cast<size_t>(wpb) * CPW * (lw + rw) * 4;
     const int tw = table_stage_words<Pairs>(b, chains);

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batc
     double *eo = avg + S;
     Real *e = reinterpret_cast<Real *>(eo + S);   // site energies (electrodes: voltages)
     float *of = reinterpret_cast<float *>(e + S);  // FP32 copy of the probabilities
-    __shared__ double sh_tot, sh_mc, sh_time;
+    __shared__ double sh_f, sh_ts, sh_time;
     __shared__ int sh_stop;
 
     // pair tables: K = nu*tc, B = I_0 R / d between acceptors (0 otherwise)
@@ -218,14 +218,15 @@ __global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batc
         }
         __syncthreads();
 
-        // (4) total and step size
+        // (4) total and step size (one warp; one FP64 division per iteration)
         if (warp == 0) {
             double tot = 0.0;
             for (int k = lane; k < S; k += 32) tot += outs[k];
             tot = warp_sum(tot);
+            const double inv = 1.0 / tot;
             double mc = 1.0;
             for (int k = lane; k < N; k += 32) {
-                const double q = (ins[k] - outs[k]) / tot;
+                const double q = (ins[k] - outs[k]) * inv;
                 const double nv = occ[k] + q;
                 if (nv < 0) mc = fmin(mc, occ[k] / -q);
                 if (nv > 1) mc = fmin(mc, (1.0 - occ[k]) / q);
@@ -235,9 +236,9 @@ __global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batc
                 if (!(tot > 0.0) || !(tot < 1.0e300)) {
                     sh_stop = 1;
                 } else {
-                    sh_tot = tot;
-                    sh_mc = mc;
-                    sh_time += 0.98 * mc / tot;
+                    sh_f = mc * inv;              // fraction of each expected flow moved
+                    sh_ts = 0.98 * mc * inv;      // time step
+                    sh_time += sh_ts;
                 }
             }
         }
@@ -245,8 +246,8 @@ __global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batc
         if (sh_stop) break;
 
         // (5) move the expected charge, record, clamp
-        const double f = sh_mc / sh_tot;
-        const double ts = 0.98 * sh_mc / sh_tot;
+        const double f = sh_f;
+        const double ts = sh_ts;
         for (int k = tid; k < S; k += kMfThreads) {
             const double net = ins[k] - outs[k];
             if (k < N) {

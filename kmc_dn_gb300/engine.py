@@ -460,10 +460,19 @@ class Batch:
         self.launch(None, stream)
         return self
 
-    def results(self):
+    def results(self, stream=None):
         """Copy results to the host: dict of numpy arrays (ragged per chain
-        lists for occupations and electrode counts)."""
+        lists for occupations and electrode counts).  With `stream`, wait for
+        that stream only (the one this batch was launched on) and copy on it;
+        otherwise synchronise the device."""
+        if stream is not None:
+            with torch.cuda.stream(stream):
+                stream.synchronize()
+                return self._results()
         torch.cuda.synchronize(self.dev)
+        return self._results()
+
+    def _results(self):
         eo = self.electrode_occupation.cpu().numpy()
         occ = self.occupation.cpu().numpy()
         out = dict(time=self.time.cpu().numpy(), status=self.status.cpu().numpy(),

@@ -12,14 +12,20 @@ seed.  The server
   so a request only ships its voltages; the constant site energies of its
   chains are superposed on the device (``kmc_site_energies``);
 * admits waiting requests, least work first (chains x hops x pairs per
-  hop), while their chain state fits the device memory budget and the
-  number of resident chains stays below what keeps the device busy without
-  time-slicing everything; admitted state stays resident until the request
-  is done;
-* runs every admitted request in quanta of hops on a pool of CUDA streams,
-  so requests that arrive while others run are started at once and their
-  launches overlap on the device; the request with the least remaining work
-  is launched first and short requests use the high-priority streams;
+  hop), while their chain state fits the device memory budget; long
+  requests (more than ``short_hops`` hops) may hold at most
+  ``max_active_long_chains`` resident chains -- about what fills the
+  device's chain slots -- so a short request is admitted on arrival
+  instead of queueing behind minutes of long work; admitted state stays
+  resident until the request is done;
+* runs every admitted request in quanta of hops on a CUDA stream of its own
+  (pooled and reused), so requests that arrive while others run are started
+  at once, their launches overlap on the device, and reading a finished
+  request's results waits for nothing else; the request with the least
+  remaining work is launched first, short requests use high-priority
+  streams and wider thread groups, and long requests run in shorter quanta
+  so that the blocks a short request waits for free up within a few
+  milliseconds;
 * returns per-chain currents, times and electrode counts, and records each
   request's latency (arrival to result on the host).
 
@@ -74,35 +80,47 @@ class Server:
     """Serve hop-loop requests on one GPU with continuous batching.
 
     networks:       list of workloads.Network (the resident geometries)
-    quantum:        hops per launch and request (a multiple of 1024)
+    quantum:        hops per launch of a short request (a multiple of 1024)
+    quantum_long:   hops per launch of a long request (default 1024)
+    short_lanes_factor: short requests run with this many times the default
+                    threads per chain (lower latency, lower throughput)
+    short_hops:     requests with at most this many hops are short
+    max_active_long_chains: resident chains of long requests (default 8192)
+    max_active_chains:      resident chains in all
     mem_budget:     bytes of chain state admitted at once (default: a
                     quarter of the free device memory at start)
-    n_streams:      CUDA streams launches are spread over
     pair_mode:      "positions" (tables must be those of the positions) or
                     "table"
     """
 
-    def __init__(self, networks, *, quantum=4096, mem_budget=None, n_streams=8,
+    def __init__(self, networks, *, quantum=4096, mem_budget=None,
                  pair_mode="positions", lanes=None, dev=None, short_hops=20000,
-                 max_active_chains=16384):
-        if quantum % _REANCHOR:
-            raise ValueError("quantum must be a multiple of the re-anchor period (1024)")
+                 max_active_chains=16384, max_active_long_chains=8192, quantum_long=_REANCHOR,
+                 short_lanes_factor=4):
+        if quantum % _REANCHOR or quantum_long % _REANCHOR or quantum_long <= 0:
+            raise ValueError("quantum and quantum_long must be multiples of the re-anchor period (1024)")
         d = torch.device(dev if dev is not None else "cuda")
         self.dev = torch.device("cuda", d.index if d.index is not None else torch.cuda.current_device())
         self.networks = list(networks)
         self.quantum = int(quantum)
+        self.quantum_long = int(quantum_long)
         self.pair_mode = pair_mode
         self.lanes = lanes
+        self.short_lanes_factor = int(short_lanes_factor)
         self.short_hops = int(short_hops)
         free, _total = torch.cuda.mem_get_info(self.dev)
         self.mem_budget = int(mem_budget if mem_budget is not None else free // 4)
         self.mem_used = 0
         self.max_active_chains = int(max_active_chains)
+        self.max_active_long_chains = int(max_active_long_chains)
         self.active_chains = 0
+        self.active_long_chains = 0
         lo, hi = torch.cuda.Stream.priority_range()
-        self.hi_streams = [torch.cuda.Stream(device=self.dev, priority=hi) for _ in range(max(1, n_streams // 2))]
-        self.lo_streams = [torch.cuda.Stream(device=self.dev, priority=lo) for _ in range(max(1, n_streams - n_streams // 2))]
-        self._rr = 0
+        # every active request owns a stream (no request waits behind another's
+        # launches); finished requests return theirs to a pool per priority
+        self._prio = {True: hi, False: lo}
+        self._free_streams = {True: [], False: []}
+        self.n_streams_created = 0
         self.specs = [TableSpec.from_network(n) for n in self.networks]
         # one resident table set per geometry (a request names one geometry)
         self.table_sets = [TableSet([sp], pair_mode=pair_mode, dev=self.dev) for sp in self.specs]
@@ -118,6 +136,7 @@ class Server:
         self._stop = False
         self._error = None
         self.hops_done = 0
+        self.launches = 0         # kernels launched (site energies + engine)
 
     # ---------------------------------------------------------------- API
     def submit(self, geometry, voltages, hops, seed):
@@ -180,6 +199,18 @@ class Server:
         pairs = h * (net.N - h) + h * net.P + net.P * (net.N - h)
         return req.voltages.shape[0] * req.hops * pairs
 
+    def _lanes(self, req):
+        """Threads per chain: the throughput default, or for a short request
+        a wider group (its latency is hops x per-hop time, and a wider group
+        cuts the per-hop time)."""
+        if self.lanes is not None:
+            return self.lanes
+        if req.hops > self.short_hops or self.short_lanes_factor <= 1:
+            return None
+        from .engine import default_lanes
+        net = self.networks[req.geometry]
+        return min(512, default_lanes(net.N + net.P) * self.short_lanes_factor)
+
     def _admit(self):
         if not self.queue:
             return
@@ -188,9 +219,12 @@ class Server:
             net = self.networks[req.geometry]
             n = req.voltages.shape[0]
             need = _request_bytes(n, net.N, net.P)
-            if self.active and (self.mem_used + need > self.mem_budget or
-                                self.active_chains + n > self.max_active_chains):
-                break
+            long_ = req.hops > self.short_hops
+            if self.active:
+                if self.mem_used + need > self.mem_budget or self.active_chains + n > self.max_active_chains:
+                    break
+                if long_ and self.active_long_chains + n > self.max_active_long_chains:
+                    continue        # a shorter request further down may still fit
             self.queue.remove(req)
             self._prepare(req, need)
 
@@ -198,18 +232,24 @@ class Server:
         net = self.networks[req.geometry]
         n = req.voltages.shape[0]
         short = req.hops <= self.short_hops
-        pool = self.hi_streams if short else self.lo_streams
-        req.stream = pool[self._rr % len(pool)]
-        self._rr += 1
+        pool = self._free_streams[short]
+        if pool:
+            req.stream = pool.pop()
+        else:
+            req.stream = torch.cuda.Stream(device=self.dev, priority=self._prio[short])
+            self.n_streams_created += 1
         with torch.cuda.stream(req.stream):
             ec, ve = superpose(net.basis, net.comp, req.voltages, net.mu, dev=self.dev, stream=req.stream)
             req.batch = Batch(self.table_sets[req.geometry], np.zeros(n, np.int32), np.full(n, net.kT), None, None,
                               np.tile(net.occupation.astype(np.uint8), (n, 1)), np.full(n, req.hops),
-                              seed=req.seed, lanes=self.lanes, dev=self.dev, E_constant_dev=ec,
+                              seed=req.seed, lanes=self._lanes(req), dev=self.dev, E_constant_dev=ec,
                               el_energy_dev=ve, pair_mode=self.pair_mode)
+        self.launches += 1
         req.bytes = need
         self.mem_used += need
         self.active_chains += n
+        if req.hops > self.short_hops:
+            self.active_long_chains += n
         self.active.append(req)
 
     def _launch_ready(self):
@@ -219,10 +259,12 @@ class Server:
                 continue
             if req.inflight is not None and not req.inflight.query():
                 continue
-            seg = min(self.quantum, req.hops - req.launched_hops)
+            q = self.quantum if req.hops <= self.short_hops else self.quantum_long
+            seg = min(q, req.hops - req.launched_hops)
             seg_launch = ((seg + _REANCHOR - 1) // _REANCHOR) * _REANCHOR
             with torch.cuda.stream(req.stream):
                 req.batch.launch(seg_launch, stream=req.stream)
+                self.launches += len(req.batch._bins)
                 ev = torch.cuda.Event()
                 ev.record(req.stream)
             req.inflight = ev
@@ -233,7 +275,7 @@ class Server:
         still = []
         for req in self.active:
             if req.launched_hops >= req.hops and req.inflight is not None and req.inflight.query():
-                r = req.batch.results()
+                r = req.batch.results(stream=req.stream)
                 cur = np.array([e / t if t > 0 else np.full(len(e), np.nan)
                                 for e, t in zip(r["electrode_occupation"], r["time"])])
                 req.done_at = time.perf_counter()
@@ -242,7 +284,10 @@ class Server:
                            status=r["status"], latency=req.done_at - req.arrival)
                 self.mem_used -= req.bytes
                 self.active_chains -= req.voltages.shape[0]
+                if req.hops > self.short_hops:
+                    self.active_long_chains -= req.voltages.shape[0]
                 req.batch = None
+                self._free_streams[req.hops <= self.short_hops].append(req.stream)
                 self.finished.append(req)
                 req.future.set_result(out)
             else:

@@ -66,3 +66,19 @@ def test_latency_summary(engine_lib):
     s = latency_summary(reqs)
     assert s["all"]["n"] == 6 and s["hops_2000"]["n"] == 3
     assert s["all"]["p99_ms"] >= s["all"]["p50_ms"] > 0
+
+
+def test_short_requests_bypass_the_long_chain_cap(engine_lib):
+    """Long requests hold at most max_active_long_chains resident chains; a
+    short request is admitted beside them at once."""
+    srv, nets = _server(quantum=2048, max_active_long_chains=64, short_hops=4096)
+    longs = [srv.submit(0, np.zeros((64, 8)), 8192, seed=i) for i in range(2)]
+    short = srv.submit(0, np.zeros((16, 8)), 2048, seed=9)
+    with srv.lock:
+        srv._admit()
+        admitted = set(id(r) for r in srv.active)
+    assert id(short) in admitted and id(longs[0]) in admitted and id(longs[1]) not in admitted
+    assert srv.active_long_chains == 64
+    srv.run_sync()
+    assert all(np.all(r.future.result()["status"] == 0) for r in longs + [short])
+    assert srv.active_long_chains == 0 and srv.active_chains == 0
