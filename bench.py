@@ -258,14 +258,16 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
 
+    from kmc_dn_gb300.parallel import replica_chains, reduce_step
     n_chains, hops = args.chains, args.hops
-    net, V = build_workload(args.seed, n_chains, chain_offset=rank * n_chains)
+    chain_offset, stream_ids = replica_chains(rank, n_chains)
+    net, V = build_workload(args.seed, n_chains, chain_offset=chain_offset)
     spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
     ec_dev, vel_dev = superpose(net.basis, net.comp, V, net.mu, dev=dev)
     occ0 = np.tile(net.occupation.astype(np.uint8), (n_chains, 1))
     lanes = args.lanes if args.lanes else None
     b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT), None, None, occ0,
-              np.full(n_chains, hops), streams=np.arange(n_chains) + rank * n_chains, seed=args.seed + 1,
+              np.full(n_chains, hops), streams=stream_ids, seed=args.seed + 1,
               lanes=lanes, warps_per_block=args.warps_per_block, dev=dev, E_constant_dev=ec_dev,
               el_energy_dev=vel_dev)
     occ_init = b.occupation.clone()
@@ -319,12 +321,8 @@ def main():
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - wall0
     clocks = clk.summary()
-    total_ms = float(np.sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * hops_per_step * args.steps / (total_ms * 1e-3)
+    total_ms, job_hops = reduce_step(float(np.sum(step_ms)), hops_per_step * args.steps, device=dev)
+    value = job_hops / (total_ms * 1e-3)
     ms_per_step = total_ms / args.steps
 
     # roofline: allowed pairs (one ex2 each) per launch / launch time vs measured ex2 rate
@@ -428,10 +426,12 @@ def run_e2e(net, V, hops, seed, lanes):
     assert np.all(st == 0)
     # bytes kmc_run_batch_host copies each call (its FP32 staging of the
     # energies, the FP64 geometry tables, per-chain parameters and offsets)
-    G = lanes or (8 if N + P <= 48 else 16 if N + P <= 96 else 32)
-    n_work = (n + 32 // G - 1) // (32 // G)
+    from kmc_dn_gb300.engine import default_lanes
+    G = lanes or default_lanes(N + P)
+    cpw = max(1, 32 // G)
+    n_work = (n + cpw - 1) // cpw
     h2d = (d.nbytes + tc.nbytes + 4 * n * N + 4 * n * P + 4 * n + 4 + 4 + 8 + 4 * n + 8 * n + 8 * n
-           + occ.nbytes + hops_a.nbytes + 8 * n + 4 * n_work * (32 // G))
+           + occ.nbytes + hops_a.nbytes + 8 * n + 4 * n_work * cpw)
     d2h = t_out.nbytes + eo.nbytes + occ.nbytes + st.nbytes
     return {"value": n * hops / dt, "unit": "hops/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "api": "kmc_run_batch_host (C ABI, host buffers)"}

@@ -41,11 +41,14 @@ int ok()
 // Automatic lanes-per-chain: enough lanes that a chain's pair loop stays
 // short, few enough that per-hop group overhead (scans, FP64 compare) is
 // shared by several chains per warp.
+// Threads per chain by network size, as measured best on GB300: warp
+// slices for small networks, whole blocks for large ones.
 static int auto_lanes(int S)
 {
-    if (S <= 48) return 8;
-    if (S <= 96) return 16;
-    return 32;
+    if (S <= 48) return 16;
+    if (S <= 128) return 32;
+    if (S <= 512) return 128;
+    return 256;
 }
 
 int host_run(const HostRun &h)
@@ -111,9 +114,9 @@ int host_run(const HostRun &h)
         streams[c] = h.streams ? h.streams[c] : static_cast<uint64_t>(c);
     }
     const int G = lanes_per_chain > 0 ? lanes_per_chain : auto_lanes(Smax);
-    if (G != 4 && G != 8 && G != 16 && G != 32)
+    if (G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128 && G != 256 && G != 512)
         return fail(KMC_ERR_INVALID, "run_batch_host: lanes_per_chain %d", G);
-    const int CPW = 32 / G;
+    const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
     std::vector<int32_t> order(n_chains);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -257,7 +260,7 @@ int host_run(const HostRun &h)
     b.occ_since = d_os;
     b.traffic = d_tr;
     b.reanchor = reanchor;
-    b.warps_per_block = 4;
+    b.warps_per_block = 8;
     b.max_hops_per_launch = seg;
     b.seed = seed;
     int rc = run_batch(b, st);

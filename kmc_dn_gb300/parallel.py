@@ -15,7 +15,7 @@ import numpy as np
 
 from .engine import Batch, TableSpec
 
-__all__ = ["parrallelSimulation", "shard_range"]
+__all__ = ["parrallelSimulation", "shard_range", "replica_chains", "reduce_step"]
 
 
 class parrallelSimulation:
@@ -61,3 +61,28 @@ def shard_range(n_items, rank, world):
     base, extra = divmod(int(n_items), int(world))
     start = rank * base + min(rank, extra)
     return start, start + base + (1 if rank < extra else 0)
+
+
+def replica_chains(rank, n_chains):
+    """Replica layout over ranks (one process per GPU, weak scaling): rank r
+    runs chains [r*n, (r+1)*n) of the ensemble, with those global indices as
+    their random-stream ids, so no two ranks draw the same stream and the
+    union over ranks is one larger ensemble.  Returns (chain_offset,
+    stream_ids)."""
+    off = int(rank) * int(n_chains)
+    return off, np.arange(n_chains, dtype=np.int64) + off
+
+
+def reduce_step(total_ms, hops, device=None):
+    """Whole-job figures of a timed region across ranks: the slowest rank's
+    time and the hops of all ranks (one all-reduce each; no collective runs
+    inside the timed region).  Single process: returned unchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(total_ms), int(hops)
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    h = torch.tensor([int(hops)], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(h, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(h.item())

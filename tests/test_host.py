@@ -53,3 +53,45 @@ def test_serving_queue_removes_requests_by_identity():
     q = deque([a, b])
     q.remove(b)
     assert list(q) == [a] and a != Request(0, np.zeros((3, 8)), 10, 1, arrival=0.0)
+
+
+def _replica_rank(rank, world, port, out_dir):
+    import json
+    import os
+    import torch.distributed as dist
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.parallel import reduce_step, replica_chains
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        n = 8
+        off, sid = replica_chains(rank, n)
+        net, V = workloads.homogeneous_ensemble(n + off, 0)
+        ms, hops = reduce_step(10.0 * (rank + 1), 1000 * (rank + 1))
+        ids = [None] * world
+        dist.all_gather_object(ids, sid.tolist())
+        with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
+            json.dump(dict(off=off, sid=sid.tolist(), V=V[off:off + n].tolist(), ms=ms, hops=hops, ids=ids), f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replicas_over_two_gloo_ranks(tmp_path):
+    """The multi-GPU layout (one replica of the ensemble per rank, weak
+    scaling) over two gloo ranks on the CPU: disjoint random streams, each
+    rank's chains are its slice of one larger ensemble, and the whole-job
+    reduction takes the slowest rank's time and every rank's hops."""
+    import json
+    import socket
+    import torch.multiprocessing as mp
+    from kmc_dn_gb300 import workloads
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    mp.start_processes(_replica_rank, args=(2, port, str(tmp_path)), nprocs=2, start_method="spawn")
+    r = [json.load(open(tmp_path / f"rank{k}.json")) for k in range(2)]
+    assert set(r[0]["sid"]).isdisjoint(r[1]["sid"])
+    assert r[0]["ids"] == r[1]["ids"] == [r[0]["sid"], r[1]["sid"]]
+    _, V = workloads.homogeneous_ensemble(16, 0)
+    np.testing.assert_array_equal(np.array(r[0]["V"] + r[1]["V"]), V)
+    for k in range(2):
+        assert r[k]["ms"] == 20.0 and r[k]["hops"] == 3000
