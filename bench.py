@@ -640,6 +640,14 @@ def bench_serving(args):
     for g in range(4):
         srv.submit(g, np.zeros((32, 8)), 2048, seed=g)
     srv.run_sync()
+    # a lone 1e4-hop request per geometry on the idle device (32 and 512
+    # chains): the latency floor the loaded figures compare with
+    isolated = {}
+    for g, net in enumerate(nets):
+        for nc in (32, 512):
+            r = srv.submit(g, rng.uniform(-1, 1, (nc, 8)), 10_000, seed=1000 + g)
+            srv.run_sync()
+            isolated[f"N{net.N}_chains{nc}_ms"] = 1e3 * (r.done_at - r.arrival)
     srv.finished.clear()
     srv.hops_done = 0
     srv.start()
@@ -667,7 +675,7 @@ def bench_serving(args):
                        "requests": int(n_req), "completed": len(done), "drained": bool(drained),
                        "quantum_hops": srv.quantum, "quantum_long_hops": srv.quantum_long,
                        "max_active_long_chains": srv.max_active_long_chains},
-            "latency": lat, "gpu_launches": srv.launches}
+            "latency": lat, "latency_isolated_1e4_hops": isolated, "gpu_launches": srv.launches}
 
 
 if __name__ == "__main__":

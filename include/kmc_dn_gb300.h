@@ -268,6 +268,37 @@ int kmc_run_batch_host(int32_t n_geoms, const int32_t *geom_N, const int32_t *ge
                        int64_t *electrode_occupation, int32_t *status);
 
 /* ------------------------------------------------------------------------ */
+/* Resident engine handle: chain state stays on the device between runs     */
+/* (the resident / serving mode; the reference has no counterpart -- its Go  */
+/* calls, simulationWrapper.go:83-315, rebuild every state per call)        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct kmc_engine kmc_engine;
+
+/* Upload the geometries and chains (arguments as kmc_run_batch_host, host
+ * buffers; record = KMC_RECORD_*) and keep them resident.  stream NULL: the
+ * engine creates its own.  Nothing runs yet. */
+int kmc_engine_create(kmc_engine **engine, int32_t n_geoms, const int32_t *geom_N, const int32_t *geom_P,
+                      const double *geom_nu, const double *geom_I0, const double *geom_R,
+                      const int64_t *geom_pair_off, const double *distances,
+                      const double *transitions_constant, int32_t n_chains, const int32_t *chain_geom,
+                      const double *chain_kT, const double *E_constant, const double *site_energies,
+                      const uint8_t *occupation, const int64_t *hops, uint64_t seed,
+                      int32_t lanes_per_chain, int32_t record, void *stream);
+/* Advance every chain by up to max_hops more hops (rounded up to 1024; <= 0:
+ * to its budget), asynchronously.  A run split into several calls gives the
+ * results of a single call. */
+int kmc_engine_run(kmc_engine *engine, int64_t max_hops);
+/* Copy the current results to host buffers (any may be NULL) and wait for
+ * the engine: time[n_chains], electrode_occupation[sum P], occupation
+ * [sum N], status[n_chains], hops_done[n_chains]; with record, traffic
+ * (S*S per chain, chain order) and occupations_in_time (N per chain). */
+int kmc_engine_read(kmc_engine *engine, double *time_out, int64_t *electrode_occupation, uint8_t *occupation,
+                    int32_t *status, int64_t *hops_done, double *traffic, double *occupations_in_time);
+/* Free the engine's device memory (waits for its work). */
+void kmc_engine_destroy(kmc_engine *engine);
+
+/* ------------------------------------------------------------------------ */
 /* Mean-field relaxation (replaces probSimulate / wrapperSimulateProbability, */
 /* goSimulation/probabilitySimulation.go:53-157, simulationWrapper.go:224-235) */
 /* ------------------------------------------------------------------------ */

@@ -92,6 +92,11 @@ _SIGS = {
     "kmc_measure_ex2_rate": (C.c_int, [C.POINTER(_f64)]),
     "kmc_run_batch_host": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _u64, _i32, _vp, _vp, _vp]),
+    "kmc_engine_create": (C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp,
+                                    _vp, _vp, _vp, _u64, _i32, _i32, _vp]),
+    "kmc_engine_run": (C.c_int, [_vp, _i64]),
+    "kmc_engine_read": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "kmc_engine_destroy": (None, [_vp]),
     "kmc_mf_max_sites": (_i32, [_i32]),
     "kmc_mf_smem_bytes": (_sz, [_i32, _i32]),
     "kmc_mf_run": (C.c_int, [C.POINTER(KmcMfBatch), _vp]),

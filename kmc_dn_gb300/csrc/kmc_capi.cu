@@ -3,6 +3,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
 #include <numeric>
 #include <vector>
 
@@ -51,8 +54,32 @@ static int auto_lanes(int S)
     return 256;
 }
 
-int host_run(const HostRun &h)
+// A batch of chains resident on the device: tables, per-chain state and the
+// launch description, advanced by run() any number of times (a run split
+// into launches gives the results of one launch: quanta start at multiples
+// of the re-anchor period and the random streams are counter-based).
+struct EngineState {
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::vector<void *> ptrs;
+    kmc_batch b;
+    int32_t n_chains = 0;
+    int64_t nsite = 0, nel = 0, npair = 0, maxhops = 0;
+    int record = 0;
+    std::mutex mu;
+    ~EngineState()
+    {
+        for (void *p : ptrs) cudaFreeAsync(p, st);
+        if (st) {
+            cudaStreamSynchronize(st);
+            if (own_stream) cudaStreamDestroy(st);
+        }
+    }
+};
+
+int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
 {
+    *out = nullptr;
     const int32_t n_geoms = h.n_geoms;
     const int32_t *geom_N = h.geom_N, *geom_P = h.geom_P;
     const double *geom_nu = h.geom_nu, *geom_I0 = h.geom_I0, *geom_R = h.geom_R;
@@ -61,27 +88,22 @@ int host_run(const HostRun &h)
     const int32_t n_chains = h.n_chains;
     const int32_t *chain_geom = h.chain_geom;
     const double *chain_kT = h.chain_kT, *E_constant = h.E_constant, *site_energies_in = h.site_energies;
-    uint8_t *occupation = h.occupation;
+    const uint8_t *occupation = h.occupation;
     const int64_t *hops = h.hops;
-    const uint64_t seed = h.seed;
-    const int32_t lanes_per_chain = h.lanes_per_chain;
-    double *time_out = h.time_out;
-    int64_t *electrode_occupation = h.electrode_occupation;
-    int32_t *status = h.status;
     const int record = h.record;
-    if (n_geoms <= 0 || n_chains < 0) return fail(KMC_ERR_INVALID, "run_batch_host: bad counts");
+    if (n_geoms <= 0 || n_chains <= 0) return fail(KMC_ERR_INVALID, "engine: bad counts");
+    if (record < 0 || record > 2) return fail(KMC_ERR_INVALID, "engine: bad record mode %d", record);
     if (!geom_N || !geom_P || !geom_nu || !geom_I0 || !geom_R || !geom_pair_off || !distances ||
-        !transitions_constant || (n_chains > 0 && (!chain_geom || !chain_kT || !E_constant ||
-        !site_energies_in || !occupation || !hops || !time_out || !electrode_occupation || !status)))
-        return fail(KMC_ERR_INVALID, "run_batch_host: NULL pointer");
-    if (n_chains == 0) return KMC_OK;
+        !transitions_constant || !chain_geom || !chain_kT || !E_constant || !site_energies_in ||
+        !occupation || !hops)
+        return fail(KMC_ERR_INVALID, "engine: NULL pointer");
     int Smax = 0;
     std::vector<int64_t> tab_off(n_geoms);
     int64_t tab_floats = 0, pair_total = 0;
     for (int g = 0; g < n_geoms; ++g) {
         const int S = geom_N[g] + geom_P[g];
         if (geom_N[g] < 0 || geom_P[g] < 0 || geom_P[g] > 64 || S <= 0 || S > kMaxSitesF32)
-            return fail(KMC_ERR_INVALID, "run_batch_host: geometry %d has N=%d P=%d", g, geom_N[g], geom_P[g]);
+            return fail(KMC_ERR_INVALID, "engine: geometry %d has N=%d P=%d", g, geom_N[g], geom_P[g]);
         tab_off[g] = tab_floats;
         tab_floats += 2 * (int64_t)S * S;
         pair_total = std::max<int64_t>(pair_total, geom_pair_off[g] + (int64_t)S * S);
@@ -90,8 +112,8 @@ int host_run(const HostRun &h)
     int64_t nsite = 0, nel = 0, nsev = 0, maxhops = 0;
     for (int c = 0; c < n_chains; ++c) {
         const int g = chain_geom[c];
-        if (g < 0 || g >= n_geoms) return fail(KMC_ERR_INVALID, "run_batch_host: chain %d geometry %d", c, g);
-        if (hops[c] < 0 || !(chain_kT[c] > 0)) return fail(KMC_ERR_INVALID, "run_batch_host: chain %d hops/kT", c);
+        if (g < 0 || g >= n_geoms) return fail(KMC_ERR_INVALID, "engine: chain %d geometry %d", c, g);
+        if (hops[c] < 0 || !(chain_kT[c] > 0)) return fail(KMC_ERR_INVALID, "engine: chain %d hops/kT", c);
         Smax = std::max(Smax, geom_N[g] + geom_P[g]);
         site_off[c] = nsite;
         el_off[c] = nel;
@@ -113,9 +135,9 @@ int host_run(const HostRun &h)
         tabid[c] = g;
         streams[c] = h.streams ? h.streams[c] : static_cast<uint64_t>(c);
     }
-    const int G = lanes_per_chain > 0 ? lanes_per_chain : auto_lanes(Smax);
+    const int G = h.lanes_per_chain > 0 ? h.lanes_per_chain : auto_lanes(Smax);
     if (G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128 && G != 256 && G != 512)
-        return fail(KMC_ERR_INVALID, "run_batch_host: lanes_per_chain %d", G);
+        return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d", G);
     const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
     std::vector<int32_t> order(n_chains);
     std::iota(order.begin(), order.end(), 0);
@@ -128,29 +150,33 @@ int host_run(const HostRun &h)
     const int n_work = (n_chains + CPW - 1) / CPW;
     std::vector<int32_t> work((size_t)n_work * CPW, -1);
     for (int c = 0; c < n_chains; ++c) work[c] = order[c];
-    const int reanchor = 1024;
-    int64_t seg = ((maxhops + reanchor - 1) / reanchor) * reanchor;
-    if (seg <= 0) seg = reanchor;
+    std::vector<int64_t> poff(n_chains);
+    int64_t npair = 0;
+    for (int c = 0; c < n_chains; ++c) {
+        const int S = geom_N[chain_geom[c]] + geom_P[chain_geom[c]];
+        poff[c] = npair;
+        npair += (int64_t)S * S;
+    }
 
-    cudaStream_t st;
-    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return fail_cuda(e, "run_batch_host: stream");
-    struct Dev {
-        std::vector<void *> ptrs;
-        cudaStream_t st;
-        ~Dev() {
-            for (void *p : ptrs) cudaFreeAsync(p, st);
-            cudaStreamSynchronize(st);
-            cudaStreamDestroy(st);
-        }
-    } dev{{}, st};
+    EngineState *E = new (std::nothrow) EngineState();
+    if (!E) return fail(KMC_ERR_OOM, "engine: host allocation");
+    std::unique_ptr<EngineState> guard(E);
+    cudaError_t e;
+    if (user_stream) {
+        E->st = user_stream;
+    } else {
+        if ((e = cudaStreamCreateWithFlags(&E->st, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail_cuda(e, "engine: stream");
+        E->own_stream = true;
+    }
+    cudaStream_t st = E->st;
     auto dalloc = [&](void **p, size_t bytes) -> cudaError_t {
         cudaError_t r = cudaMallocAsync(p, bytes ? bytes : 16, st);
-        if (r == cudaSuccess) dev.ptrs.push_back(*p);
+        if (r == cudaSuccess) E->ptrs.push_back(*p);
         return r;
     };
-    auto h2d = [&](void *d, const void *h, size_t bytes) {
-        return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
+    auto h2d = [&](void *d, const void *hp, size_t bytes) {
+        return cudaMemcpyAsync(d, hp, bytes, cudaMemcpyHostToDevice, st);
     };
     double *d_dist = nullptr, *d_tc = nullptr;
     float *d_tab = nullptr, *d_ec = nullptr, *d_vel = nullptr, *d_kT = nullptr;
@@ -163,13 +189,6 @@ int host_run(const HostRun &h)
     int64_t *d_poff = nullptr;
     double *d_ot = nullptr, *d_os = nullptr;
     int32_t *d_tr = nullptr;
-    std::vector<int64_t> poff(n_chains);
-    int64_t npair = 0;
-    for (int c = 0; c < n_chains; ++c) {
-        const int S = geom_N[chain_geom[c]] + geom_P[chain_geom[c]];
-        poff[c] = npair;
-        npair += (int64_t)S * S;
-    }
     const size_t pair_bytes = sizeof(double) * (size_t)pair_total;
     if ((e = dalloc((void **)&d_dist, pair_bytes)) != cudaSuccess ||
         (e = dalloc((void **)&d_tc, pair_bytes)) != cudaSuccess ||
@@ -191,17 +210,17 @@ int host_run(const HostRun &h)
         (e = dalloc((void **)&d_stream, sizeof(uint64_t) * n_chains)) != cudaSuccess ||
         (e = dalloc((void **)&d_status, sizeof(int32_t) * n_chains)) != cudaSuccess ||
         (e = dalloc((void **)&d_work, sizeof(int32_t) * work.size())) != cudaSuccess)
-        return fail_cuda(e, "run_batch_host: device allocation");
+        return fail_cuda(e, "engine: device allocation");
     if (record) {
         if ((e = dalloc((void **)&d_poff, sizeof(int64_t) * n_chains)) != cudaSuccess ||
             (e = dalloc((void **)&d_ot, sizeof(double) * std::max<int64_t>(nsite, 1))) != cudaSuccess ||
             (e = dalloc((void **)&d_os, sizeof(double) * std::max<int64_t>(nsite, 1))) != cudaSuccess ||
             (e = dalloc((void **)&d_tr, sizeof(int32_t) * std::max<int64_t>(npair, 1))) != cudaSuccess)
-            return fail_cuda(e, "run_batch_host: record allocation");
+            return fail_cuda(e, "engine: record allocation");
         if ((e = h2d(d_poff, poff.data(), sizeof(int64_t) * n_chains)) != cudaSuccess ||
             (e = cudaMemsetAsync(d_ot, 0, sizeof(double) * std::max<int64_t>(nsite, 1), st)) != cudaSuccess ||
             (e = cudaMemsetAsync(d_tr, 0, sizeof(int32_t) * std::max<int64_t>(npair, 1), st)) != cudaSuccess)
-            return fail_cuda(e, "run_batch_host: record init");
+            return fail_cuda(e, "engine: record init");
     }
     if ((e = h2d(d_dist, distances, pair_bytes)) != cudaSuccess ||
         (e = h2d(d_tc, transitions_constant, pair_bytes)) != cudaSuccess ||
@@ -218,18 +237,20 @@ int host_run(const HostRun &h)
         (e = h2d(d_ht, hops, sizeof(int64_t) * n_chains)) != cudaSuccess ||
         (e = h2d(d_stream, streams.data(), sizeof(uint64_t) * n_chains)) != cudaSuccess ||
         (e = h2d(d_work, work.data(), sizeof(int32_t) * work.size())) != cudaSuccess)
-        return fail_cuda(e, "run_batch_host: copy in");
+        return fail_cuda(e, "engine: copy in");
     if ((e = cudaMemsetAsync(d_eo, 0, sizeof(int64_t) * std::max<int64_t>(nel, 1), st)) != cudaSuccess ||
         (e = cudaMemsetAsync(d_time, 0, sizeof(double) * n_chains, st)) != cudaSuccess ||
         (e = cudaMemsetAsync(d_hd, 0, sizeof(int64_t) * n_chains, st)) != cudaSuccess)
-        return fail_cuda(e, "run_batch_host: memset");
+        return fail_cuda(e, "engine: memset");
     for (int g = 0; g < n_geoms; ++g) {
         const int rc = build_table(geom_N[g], geom_P[g], geom_nu[g], geom_I0[g], geom_R[g],
                                    d_dist + geom_pair_off[g], d_tc + geom_pair_off[g],
                                    d_tab + tab_off[g], st);
         if (rc != KMC_OK) return rc;
     }
-    kmc_batch b;
+    // the FP64 source tables are needed only to build the FP32 ones
+    // (freed with the engine; stream order keeps them alive for build_table)
+    kmc_batch &b = E->b;
     memset(&b, 0, sizeof(b));
     b.n_tables = n_geoms;
     b.max_sites = Smax;
@@ -259,33 +280,80 @@ int host_run(const HostRun &h)
     b.occ_time = d_ot;
     b.occ_since = d_os;
     b.traffic = d_tr;
-    b.reanchor = reanchor;
+    b.reanchor = 1024;
     b.warps_per_block = 8;
-    b.max_hops_per_launch = seg;
-    b.seed = seed;
-    int rc = run_batch(b, st);
-    if (rc != KMC_OK) return rc;
-    if ((e = cudaMemcpyAsync(time_out, d_time, sizeof(double) * n_chains, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(electrode_occupation, d_eo, sizeof(int64_t) * nel, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(occupation, d_occ, (size_t)nsite, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(status, d_status, sizeof(int32_t) * n_chains, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-        return fail_cuda(e, "run_batch_host: copy out");
+    b.max_hops_per_launch = 1024;
+    b.seed = h.seed;
+    E->n_chains = n_chains;
+    E->nsite = nsite;
+    E->nel = nel;
+    E->npair = npair;
+    E->maxhops = maxhops;
+    E->record = record;
+    *out = guard.release();
+    return KMC_OK;
+}
+
+// Advance every chain by up to max_hops hops (rounded up to the re-anchor
+// period; <= 0: to its budget).  Asynchronous on the engine's stream.
+int engine_run(EngineState &E, int64_t max_hops)
+{
+    const int64_t reanchor = E.b.reanchor;
+    int64_t seg = max_hops > 0 ? max_hops : E.maxhops;
+    seg = std::max<int64_t>(reanchor, ((seg + reanchor - 1) / reanchor) * reanchor);
+    E.b.max_hops_per_launch = seg;
+    return run_batch(E.b, E.st);
+}
+
+// Copy results to the host (synchronises the engine's stream).  traffic_out
+// (S*S per chain, row-major, chain order) and occ_time_out (N per chain)
+// receive the cumulative record-mode sums; any output may be NULL.
+int engine_read(EngineState &E, double *time_out, int64_t *electrode_occupation, uint8_t *occupation,
+                int32_t *status, int64_t *hops_done, double *traffic_out, double *occ_time_out)
+{
+    cudaStream_t st = E.st;
+    cudaError_t e = cudaSuccess;
+    auto d2h = [&](void *hp, const void *d, size_t bytes) {
+        if (hp && e == cudaSuccess) e = cudaMemcpyAsync(hp, d, bytes, cudaMemcpyDeviceToHost, st);
+    };
+    d2h(time_out, E.b.time, sizeof(double) * E.n_chains);
+    d2h(electrode_occupation, E.b.electrode_occupation, sizeof(int64_t) * E.nel);
+    d2h(occupation, E.b.occupation, (size_t)E.nsite);
+    d2h(status, E.b.status, sizeof(int32_t) * E.n_chains);
+    d2h(hops_done, E.b.hops_done, sizeof(int64_t) * E.n_chains);
     std::vector<int32_t> tr_h;
-    std::vector<double> ot_h;
-    if (record) {
-        tr_h.resize(std::max<int64_t>(npair, 1));
-        ot_h.resize(std::max<int64_t>(nsite, 1));
-        if ((e = cudaMemcpyAsync(tr_h.data(), d_tr, sizeof(int32_t) * tr_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(ot_h.data(), d_ot, sizeof(double) * ot_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-            return fail_cuda(e, "run_batch_host: record copy out");
+    if (E.record && traffic_out) {
+        tr_h.resize(std::max<int64_t>(E.npair, 1));
+        d2h(tr_h.data(), E.b.traffic, sizeof(int32_t) * tr_h.size());
     }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "run_batch_host: run");
-    if (record) {
-        for (int64_t k = 0; k < npair; ++k)
-            if (h.traffic_out) h.traffic_out[k] += tr_h[k];
-        for (int64_t k = 0; k < nsite; ++k)
-            if (h.occ_time_out) h.occ_time_out[k] += ot_h[k];
-    }
+    if (E.record) d2h(occ_time_out, E.b.occ_time, sizeof(double) * E.nsite);
+    if (e != cudaSuccess) return fail_cuda(e, "engine: copy out");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "engine: run");
+    if (E.record && traffic_out)
+        for (int64_t k = 0; k < E.npair; ++k) traffic_out[k] = static_cast<double>(tr_h[k]);
+    if (!E.record && occ_time_out) std::fill(occ_time_out, occ_time_out + E.nsite, 0.0);
+    return KMC_OK;
+}
+
+int host_run(const HostRun &h)
+{
+    if (h.n_chains == 0) return KMC_OK;
+    if (h.n_chains > 0 && (!h.time_out || !h.electrode_occupation || !h.status || !h.occupation))
+        return fail(KMC_ERR_INVALID, "run_batch_host: NULL pointer");
+    EngineState *E = nullptr;
+    int rc = engine_create(h, nullptr, &E);
+    if (rc != KMC_OK) return rc;
+    std::unique_ptr<EngineState> guard(E);
+    if ((rc = engine_run(*E, E->maxhops)) != KMC_OK) return rc;
+    std::vector<double> tr, ot;
+    if (h.record && h.traffic_out) tr.resize(std::max<int64_t>(E->npair, 1));
+    if (h.record && h.occ_time_out) ot.resize(std::max<int64_t>(E->nsite, 1));
+    rc = engine_read(*E, h.time_out, h.electrode_occupation, h.occupation, h.status, nullptr,
+                     tr.empty() ? nullptr : tr.data(), ot.empty() ? nullptr : ot.data());
+    if (rc != KMC_OK) return rc;
+    // the record outputs accumulate onto the caller's arrays
+    for (int64_t k = 0; k < (int64_t)tr.size() && k < E->npair; ++k) h.traffic_out[k] += tr[k];
+    for (int64_t k = 0; k < (int64_t)ot.size() && k < E->nsite; ++k) h.occ_time_out[k] += ot[k];
     return KMC_OK;
 }
 
@@ -311,7 +379,9 @@ int kmc_last_error(char *buf, size_t len)
 
 int kmc_engine_lane_options(void)
 {
-    return (1 << 2) | (1 << 3) | (1 << 4) | (1 << 5);   // bit k set: G = 2^k is compiled in
+    // bit k set: G = 2^k lanes per chain is compiled in (warp slices 4..32,
+    // block groups 64..512)
+    return (1 << 2) | (1 << 3) | (1 << 4) | (1 << 5) | (1 << 6) | (1 << 7) | (1 << 8) | (1 << 9);
 }
 
 size_t kmc_simulate_f64_workspace_size(int32_t n_sites)
@@ -389,6 +459,66 @@ int kmc_run_batch_host(int32_t n_geoms, const int32_t *geom_N, const int32_t *ge
     h.electrode_occupation = electrode_occupation;
     h.status = status;
     return host_run(h);
+}
+
+int kmc_engine_create(kmc_engine **engine, int32_t n_geoms, const int32_t *geom_N, const int32_t *geom_P,
+                      const double *geom_nu, const double *geom_I0, const double *geom_R,
+                      const int64_t *geom_pair_off, const double *distances,
+                      const double *transitions_constant, int32_t n_chains, const int32_t *chain_geom,
+                      const double *chain_kT, const double *E_constant, const double *site_energies_in,
+                      const uint8_t *occupation, const int64_t *hops, uint64_t seed,
+                      int32_t lanes_per_chain, int32_t record, void *stream)
+{
+    if (!engine) return fail(KMC_ERR_INVALID, "kmc_engine_create: NULL handle pointer");
+    *engine = nullptr;
+    HostRun h;
+    memset(&h, 0, sizeof(h));
+    h.n_geoms = n_geoms;
+    h.geom_N = geom_N;
+    h.geom_P = geom_P;
+    h.geom_nu = geom_nu;
+    h.geom_I0 = geom_I0;
+    h.geom_R = geom_R;
+    h.geom_pair_off = geom_pair_off;
+    h.distances = distances;
+    h.transitions_constant = transitions_constant;
+    h.n_chains = n_chains;
+    h.chain_geom = chain_geom;
+    h.chain_kT = chain_kT;
+    h.E_constant = E_constant;
+    h.site_energies = site_energies_in;
+    h.occupation = const_cast<uint8_t *>(occupation);   // read only here
+    h.hops = hops;
+    h.seed = seed;
+    h.lanes_per_chain = lanes_per_chain;
+    h.record = record;
+    EngineState *E = nullptr;
+    const int rc = engine_create(h, static_cast<cudaStream_t>(stream), &E);
+    if (rc == KMC_OK) *engine = reinterpret_cast<kmc_engine *>(E);
+    return rc;
+}
+
+int kmc_engine_run(kmc_engine *engine, int64_t max_hops)
+{
+    if (!engine) return fail(KMC_ERR_INVALID, "kmc_engine_run: NULL engine");
+    EngineState *E = reinterpret_cast<EngineState *>(engine);
+    std::lock_guard<std::mutex> lock(E->mu);
+    return engine_run(*E, max_hops);
+}
+
+int kmc_engine_read(kmc_engine *engine, double *time_out, int64_t *electrode_occupation, uint8_t *occupation,
+                    int32_t *status, int64_t *hops_done, double *traffic, double *occupations_in_time)
+{
+    if (!engine) return fail(KMC_ERR_INVALID, "kmc_engine_read: NULL engine");
+    EngineState *E = reinterpret_cast<EngineState *>(engine);
+    std::lock_guard<std::mutex> lock(E->mu);
+    return engine_read(*E, time_out, electrode_occupation, occupation, status, hops_done, traffic,
+                       occupations_in_time);
+}
+
+void kmc_engine_destroy(kmc_engine *engine)
+{
+    delete reinterpret_cast<EngineState *>(engine);
 }
 
 }  // extern "C"

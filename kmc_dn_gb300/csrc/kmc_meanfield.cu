@@ -70,6 +70,34 @@ template <> struct MfTypes<false> { using Real = float; using Pair = float2; };
 // (hi, lo) updated by TwoSum (Knuth), six FP32 operations per term, which
 // keeps the sum of FP32 terms to about 2^-44 relative without the FP64
 // pipe.
+// Two-float arithmetic for the FP32-rate mode's flows: TwoSum, and a sum
+// normalised so that |lo| <= ulp(hi) / 2.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 df_add(F2 x, F2 y)
+{
+    const float s = __fadd_rn(x.hi, y.hi);
+    const float bp = __fsub_rn(s, x.hi);
+    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bp)), __fsub_rn(y.hi, bp));
+    const float lo = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    const float hi = __fadd_rn(s, lo);
+    return F2{hi, __fsub_rn(lo, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ F2 warp_sum_df(F2 x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        x = df_add(x, F2{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)});
+    return x;
+}
+__device__ __forceinline__ float warp_min_f(float x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
 template <bool F64> struct Acc;
 template <> struct Acc<true> {
     double s = 0.0;
@@ -87,6 +115,7 @@ template <> struct Acc<false> {
         lo = __fadd_rn(lo, err);
     }
     __device__ __forceinline__ double value() const { return static_cast<double>(hi) + static_cast<double>(lo); }
+    __device__ __forceinline__ F2 pair() const { return F2{hi, lo}; }
 };
 
 // Row stride of the shared S x S arrays: odd, so that a thread per row
@@ -205,18 +234,74 @@ __global__ void __launch_bounds__(kMfThreads, F64 ? 4 : 8) mf_kernel(kmc_mf_batc
 
         // (3) outflows (threads 0..S-1, along rows) and inflows (threads
         // S..2S-1, down columns), each a sequential sum in a fixed order
+        // (FP32-rate mode: kept as two-float pairs in the same slots)
         for (int q = tid; q < 2 * S; q += kMfThreads) {
             Acc<F64> a;
+            const int k = q < S ? q : q - S;
             if (q < S) {
                 for (int j = 0; j < S; ++j) a.add(rt[q * SP + j]);
-                outs[q] = a.value();
             } else {
-                const int k = q - S;
                 for (int i = 0; i < S; ++i) a.add(rt[i * SP + k]);
-                ins[k] = a.value();
             }
+            double *dst = q < S ? outs : ins;
+            if constexpr (F64) dst[k] = a.value();
+            else reinterpret_cast<F2 *>(dst)[k] = a.pair();
         }
         __syncthreads();
+
+        if constexpr (!F64) {
+            // (4') total and step size in FP32 / two-float (one warp)
+            const F2 *outs2 = reinterpret_cast<const F2 *>(outs);
+            const F2 *ins2 = reinterpret_cast<const F2 *>(ins);
+            if (warp == 0) {
+                F2 tot{0.0f, 0.0f};
+                for (int k = lane; k < S; k += 32) tot = df_add(tot, outs2[k]);
+                tot = warp_sum_df(tot);
+                const float inv = 1.0f / tot.hi;
+                float mc = 1.0f;
+                for (int k = lane; k < N; k += 32) {
+                    const float q = df_add(ins2[k], F2{-outs2[k].hi, -outs2[k].lo}).hi * inv;
+                    const float o = of[k];
+                    const float nv = o + q;
+                    if (nv < 0.0f) mc = fminf(mc, o / -q);
+                    if (nv > 1.0f) mc = fminf(mc, (1.0f - o) / q);
+                }
+                mc = warp_min_f(mc);
+                if (lane == 0) {
+                    if (!(tot.hi > 0.0f) || !(tot.hi <= 3.0e38f)) {
+                        sh_stop = 1;
+                    } else {
+                        const float ff = mc * inv, tsf = 0.98f * mc * inv;
+                        sh_f = ff;
+                        sh_ts = tsf;
+                        sh_time += static_cast<double>(tsf);
+                    }
+                }
+            }
+            __syncthreads();
+            if (sh_stop) break;
+            // (5') move the expected charge (the state stays FP64), record, clamp
+            const float f = static_cast<float>(sh_f);
+            for (int k = tid; k < S; k += kMfThreads) {
+                const double d = static_cast<double>(df_add(ins2[k], F2{-outs2[k].hi, -outs2[k].lo}).hi * f);
+                if (k < N) {
+                    if (b.record) avg[k] += occ[k] * sh_ts;
+                    const double o = fmin(fmax(occ[k] + d, 0.0), 1.0);
+                    occ[k] = o;
+                    of[k] = static_cast<float>(o);
+                } else {
+                    eo[k] += d;
+                }
+            }
+            if (traffic)
+                for (int p = tid; p < SS; p += kMfThreads) {
+                    const int i = p / S, j = p - (p / S) * S;
+                    if (i >= N && j >= N) continue;
+                    traffic[p] += static_cast<double>((rt[i * SP + j] - rt[j * SP + i]) * f);
+                }
+            __syncthreads();
+            continue;
+        }
 
         // (4) total and step size (one warp; one FP64 division per iteration)
         if (warp == 0) {
