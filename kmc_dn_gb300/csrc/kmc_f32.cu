@@ -23,13 +23,15 @@
 //               positions mode, from the sites' coordinates carried in the
 //               lists (d from one rsqrt; no table traffic).
 //  selection    The per-thread sums are scanned in double-float (two FP32
-//               words, about 47 bits; GB300's FP64 rate is 1/64 of FP32);
-//               the clock advances by Exp(1)/total, accumulated the same way
-//               (simulation.go:297-298); the event is the first pair whose
-//               cumulative rate reaches u*total (kmc_dopant_networks.py:
-//               106-110), u with 47 random bits: the double-float compare
+//               words, about 47 bits: the precision the final cumulative-
+//               rate comparison needs, on the FP32 pipe, since GB300 runs
+//               FP64 at 1/64 of the FP32 rate); the event is the first pair
+//               whose cumulative rate reaches u*total (kmc_dopant_networks.
+//               py:106-110), u with 47 random bits: the double-float compare
 //               picks the thread, then that thread's stored running sums
 //               (or its re-evaluated run) are searched relative to its base.
+//               The clock advances by Exp(1)/total accumulated in FP64
+//               (simulation.go:297-298).
 //  hop          O(N) incremental energy update (makeJump,
 //               simulation.go:107-130), occupancy bits, electrode counters,
 //               optional record (numba or Go convention); every `reanchor`
@@ -83,9 +85,9 @@ __device__ __forceinline__ float rsqrt_approx(float x)
 
 // ---------------------------------------------------------------------------
 // Double-float arithmetic: a value hi + lo held in two floats.  GB300 issues
-// FP64 at 1/64 of the FP32 rate, so the per-hop scan, event target and clock
-// run in this form; TwoSum / TwoProduct (Knuth, Dekker) keep them exact to
-// about 2^-47 relative.
+// FP64 at 1/64 of the FP32 rate, so the per-hop group scan and the event
+// target run in this form; TwoSum / TwoProduct (Knuth, Dekker) keep them
+// exact to about 2^-47 relative.
 // ---------------------------------------------------------------------------
 struct F2 {
     float hi, lo;
@@ -120,8 +122,6 @@ __device__ __forceinline__ F2 df_mul(F2 x, F2 y)
 
 // x >= y for normalised values
 __device__ __forceinline__ bool df_ge(F2 x, F2 y) { return x.hi > y.hi || (x.hi == y.hi && x.lo >= y.lo); }
-
-__device__ __forceinline__ double df_to_double(F2 x) { return static_cast<double>(x.hi) + static_cast<double>(x.lo); }
 
 __device__ __forceinline__ F2 df_from_double(double v)
 {
@@ -495,7 +495,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     int h = 0;
     for (int w = 0; w < W; ++w) h += __popc(sm.occw[w]);
 
-    F2 t = df_from_double(B.time[c]);    // the clock, double-float
+    double t = B.time[c];    // the clock: FP64 (one add per hop, off the critical path)
     int64_t hop = hops_done0;
     const int64_t hop_end = hops_done0 + (todo > 0 ? todo : 0);
     int status = KMC_OK;
@@ -505,7 +505,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     double *occ_since = record ? B.occ_since + so : nullptr;
     int32_t *traffic = record ? B.traffic + B.chain_pair_off[c] : nullptr;
     if (record)
-        for (int j = g; j < N; j += G) occ_since[j] = df_to_double(t);
+        for (int j = g; j < N; j += G) occ_since[j] = t;
 
     // Energies from scratch (E_j = Ec_j - sum_{k empty} B_jk) and the ordered
     // lists built from them.  Run at the launch start and at every absolute
@@ -711,8 +711,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const int to = Pairs::kSiteInRec ? Pairs::site(sm.tgt[col]) : sm.tgt_id[col];
         // ---- clock ----
         const float dt = e1 * __frcp_rn(tot.hi);
-        const F2 t_before = t;
-        t = df_add(t, F2{dt, 0.0f});
+        const double t_before = t;
+        t += static_cast<double>(dt);
         grp.sync();   // every thread is done reading the lists and rates
         // ---- apply the hop and rebuild the lists in one pass ----
         const bool fa = from < N, tb = to < N;
@@ -760,7 +760,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             if (record) {
                 traffic[from * S + to] += 1;
                 if (record == KMC_RECORD_GO) traffic[to * S + from] -= 1;
-                const double tx = df_to_double((record == KMC_RECORD_GO) ? t : t_before);
+                const double tx = (record == KMC_RECORD_GO) ? t : t_before;
                 if (fa) occ_time[from] += tx - occ_since[from];
                 if (tb) occ_since[to] = tx;
             }
@@ -772,7 +772,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 
     // ---- write back ----
     if (record) {
-        const double td = df_to_double(t);
+        const double td = t;
         for (int j = g; j < N; j += G)
             if ((sm.occw[j >> 5] >> (j & 31)) & 1u) {
                 occ_time[j] += td - occ_since[j];
@@ -782,7 +782,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     for (int j = g; j < N; j += G) occ_g[j] = static_cast<uint8_t>((sm.occw[j >> 5] >> (j & 31)) & 1u);
     for (int e = g; e < P; e += G) B.electrode_occupation[eoff + e] += sm.eo[e];
     if (g == 0) {
-        B.time[c] = df_to_double(t);
+        B.time[c] = t;
         B.hops_done[c] = hop;
         B.status[c] = status;
         if (B.n_pairs) B.n_pairs[c] += npairs;

@@ -39,7 +39,7 @@ def test_go_compat_names_exported(engine_lib):
     load this library in place of libSimulation.so."""
     names = declared_functions("kmc_goslice_compat.h")
     assert {"wrapperSimulate", "wrapperSimulateRecord", "wrapperSimulatePruned",
-            "wrapperSimulateRecordPlus", "parallelSimulations"} <= set(names)
+            "wrapperSimulateRecordPlus", "wrapperSimulateProbability", "parallelSimulations"} <= set(names)
 
 
 def test_error_channel_without_gpu(engine_lib):
@@ -55,11 +55,36 @@ def test_error_channel_without_gpu(engine_lib):
     assert L.kmc_version() >= 100
 
 
-def test_struct_layout_matches_header():
-    """ctypes mirror of struct kmc_batch: field order and names as in the header."""
-    from kmc_dn_gb300._native import KmcBatch
+def _struct_fields(name):
     src = open(os.path.join(REPO, "include", "kmc_dn_gb300.h")).read()
-    body = src[src.index("typedef struct kmc_batch {"):src.index("} kmc_batch;")]
+    body = src[src.index(f"typedef struct {name} {{") + len(f"typedef struct {name} {{"):src.index(f"}} {name};")]
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
-    fields = re.findall(r"(\w+)\s*;", body)
-    assert fields == [f[0] for f in KmcBatch._fields_]
+    names = []
+    for stmt in body.split(";"):
+        if stmt.strip():
+            names += [re.findall(r"\w+", d)[-1] for d in stmt.split(",")]
+    return names
+
+
+def test_struct_layout_matches_header():
+    """ctypes mirrors of struct kmc_batch and struct kmc_mf_batch: field
+    order and names as in the header."""
+    from kmc_dn_gb300._native import KmcBatch, KmcMfBatch
+    assert _struct_fields("kmc_batch") == [f[0] for f in KmcBatch._fields_]
+    assert _struct_fields("kmc_mf_batch") == [f[0] for f in KmcMfBatch._fields_]
+
+
+def test_engine_handle_rejects_bad_arguments_without_gpu(engine_lib):
+    """kmc_engine_create validates its arguments before any CUDA call and
+    leaves the handle NULL; run/read on a NULL handle are errors."""
+    from kmc_dn_gb300._native import KMC_ERR_INVALID, last_error, lib
+    L = lib()
+    h = C.c_void_p()
+    # n_geoms 0, eight NULL geometry arrays, n_chains 0, six NULL chain arrays,
+    # seed, lanes, record, stream
+    assert L.kmc_engine_create(C.byref(h), 0, *([None] * 8), 0, *([None] * 6), 0, 0, 0, None) == KMC_ERR_INVALID
+    assert not h.value
+    assert L.kmc_engine_run(None, 10) == KMC_ERR_INVALID
+    assert "NULL engine" in last_error()[1]
+    assert L.kmc_engine_read(None, None, None, None, None, None, None, None) == KMC_ERR_INVALID
+    L.kmc_engine_destroy(None)          # a no-op

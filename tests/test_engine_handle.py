@@ -102,13 +102,3 @@ def test_engine_record_mode_reads_cumulative_sums(engine_lib):
         to += S[c] ** 2
         eoff += P[c]
         so += N[c]
-
-
-def test_engine_rejects_bad_arguments(engine_lib):
-    from kmc_dn_gb300._native import KMC_ERR_INVALID, last_error, lib
-    L = lib()
-    h = C.c_void_p()
-    assert L.kmc_engine_create(C.byref(h), 0, *([None] * 13), None, None, 0, 0, 0, None) == KMC_ERR_INVALID
-    assert not h.value
-    assert L.kmc_engine_run(None, 10) == KMC_ERR_INVALID
-    assert "NULL engine" in last_error()[1]

@@ -113,3 +113,19 @@ def test_current_statistics_match_fixture(engine_lib):
     sig = np.sqrt(sem ** 2 + ref_sd ** 2 / 5) + 1e-30
     z = np.abs(mean - ref_mean) / sig
     assert np.all(z < 4.0), z
+
+
+@pytest.mark.gpu
+def test_go_simulation_probability_on_the_class(engine_lib):
+    """dn_search's first stage: kmc.go_simulation(hops=1000,
+    goSpecificFunction="wrapperSimulateProbability") (dn_search.py:49-52),
+    with the bridge's int-truncated counts and current = counts / time."""
+    import oracle as O
+    dn, f = fixture_dn(1)
+    dn.go_simulation(hops=1000, goSpecificFunction="wrapperSimulateProbability", record=True)
+    ref = O.prob_simulate(dn.N, dn.P, dn.nu, dn.kT, dn.I_0, dn.R, np.full(dn.N, 0.5), dn.distances,
+                          dn.E_constant, dn.site_energies, dn.transitions_constant, 1000, record=True)
+    np.testing.assert_allclose(dn.time, ref["time"], rtol=1e-9)
+    assert dn.electrode_occupation.dtype.kind == "i"
+    np.testing.assert_allclose(dn.current, dn.electrode_occupation / dn.time)
+    np.testing.assert_allclose(dn.average_occupation, ref["average_occupation"] / ref["time"], rtol=1e-9)
