@@ -224,6 +224,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="homogeneous",
                     choices=["homogeneous", "uneven", "large", "serving", "meanfield"],
                     help="homogeneous: the headline line; the others measure the other "
@@ -468,9 +469,16 @@ def bench_uneven(args):
     setup_s = time.perf_counter() - t0
     specs = [TableSpec.from_network(net) for net, _ in nets]
     hops = np.array([h for _, h in nets], np.int64)
+    lanes, tune_s = None, 0.0
+    if not args.no_autotune:
+        # lanes per size class picked by timing short runs of each class (autotune.py)
+        from kmc_dn_gb300 import autotune
+        t0 = time.perf_counter()
+        lanes = autotune.choose([s.S for s in specs], pair_mode="positions")
+        tune_s = time.perf_counter() - t0
     b = Batch(specs, np.arange(n), [net.kT for net, _ in nets], [net.E_constant() for net, _ in nets],
               [net.electrodes[:, 3] for net, _ in nets], [net.occupation.astype(np.uint8) for net, _ in nets],
-              hops, seed=args.seed + 5, pair_mode="positions")
+              hops, seed=args.seed + 5, pair_mode="positions", lanes=lanes)
     streams = [torch.cuda.Stream() for _ in range(len(b._bins))]
     dt = _timed_launch(b, int(hops.max()), streams)
     r = b.results()
@@ -498,7 +506,10 @@ def bench_uneven(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "uneven batch: 16384 chains, one network each, N~U{10..200}, P~U{4..12}, "
                                    "hops log-uniform [1e4,1e6]", "n_chains": n, "total_hops": done,
-                       "pair_mode": "positions", "bins": bins, "host_setup_s": setup_s},
+                       "pair_mode": "positions", "bins": bins, "host_setup_s": setup_s,
+                       "lanes": "autotuned per size class" if lanes else "default by size",
+                       "autotune_s": tune_s,
+                       "autotuned": {str(k): v for k, v in getattr(lanes, "picked", {}).items()}},
             "gpu_launches": len(b._bins), "n_pairs_per_s": float(r["n_pairs"].sum()) / dt}
 
 
@@ -674,7 +685,7 @@ def bench_serving(args):
                        "rate_per_s": args.rate, "arrival_window_s": args.serve_seconds,
                        "requests": int(n_req), "completed": len(done), "drained": bool(drained),
                        "quantum_hops": srv.quantum, "quantum_long_hops": srv.quantum_long,
-                       "max_active_long_chains": srv.max_active_long_chains},
+                       "long_thread_budget": srv.long_thread_budget},
             "latency": lat, "latency_isolated_1e4_hops": isolated, "gpu_launches": srv.launches}
 
 

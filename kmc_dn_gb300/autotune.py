@@ -1,9 +1,10 @@
 """Autotuner for the batched engine's launch shape.
 
 For a size class (sites per chain) it times short runs of the engine on
-synthetic chains of that size for every lanes-per-chain G in {4, 8, 16, 32}
-and warps per block in {2, 4, 8}, on the device at hand, and keeps the
-fastest (hops/s).  Results are cached per (GPU name, size class, number of
+synthetic chains of that size for every lanes-per-chain G (warp slices 4..32
+up to 256 sites, block groups 64..512 from 48 sites) and warps per block in
+{4, 8}, on the device at hand, with the class's own chain count, and keeps
+the fastest (hops/s).  Results are cached per (GPU name, size class, number of
 chains) in a JSON file (``KMC_DN_AUTOTUNE_CACHE`` or
 ``~/.cache/kmc_dn_gb300/autotune.json``), so a workload is tuned once per
 machine.  ``choose`` returns a ``lanes`` callable for ``Batch``.
@@ -20,8 +21,8 @@ import numpy as np
 __all__ = ["tune_size_class", "choose", "size_class", "cache_path", "CANDIDATE_LANES",
            "CANDIDATE_WARPS"]
 
-CANDIDATE_LANES = (4, 8, 16, 32)
-CANDIDATE_WARPS = (2, 4, 8)
+CANDIDATE_LANES = (4, 8, 16, 32, 64, 128, 256, 512)
+CANDIDATE_WARPS = (4, 8)
 _CLASS_EDGES = (24, 48, 96, 160, 256, 512, 1024, 2048)
 _LOCK = threading.Lock()
 
@@ -64,9 +65,18 @@ def _key(gpu, sc, n_chains):
     return f"{gpu}|S<={sc}|C~{1 << max(0, int(np.ceil(np.log2(max(n_chains, 1)))))}"
 
 
-def tune_size_class(S, n_chains, hops=4096, seed=0, dev=None, verbose=False):
-    """Time every (G, warps per block) for chains of S sites; return the best
-    as dict(G, warps_per_block, hops_per_s, table)."""
+def _candidates(S):
+    """Lanes per chain worth trying for S sites: warp slices up to S=256,
+    block groups from S=48 up."""
+    c = [G for G in (4, 8, 16, 32) if S <= 256]
+    c += [G for G in (64, 128, 256, 512) if S >= 48]
+    return c
+
+
+def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pair_mode="table"):
+    """Time every candidate (G, warps per block) for n_chains chains of S
+    sites (CUDA events around one launch after a warm-up launch); return the
+    best as dict(G, warps_per_block, hops_per_s, table)."""
     import torch
     from . import workloads
     from .engine import Batch, TableSpec
@@ -77,21 +87,23 @@ def tune_size_class(S, n_chains, hops=4096, seed=0, dev=None, verbose=False):
     net = workloads.make_network(rng, N, max(0, int(round(0.1 * N))), L, L,
                                  workloads.perimeter_electrodes(L, P), voltages=rng.uniform(-1, 1, P),
                                  I_0=50.0, cells=40)
-    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    spec = TableSpec.from_network(net) if pair_mode == "positions" else \
+        TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
     table = []
-    for G in CANDIDATE_LANES:
-        for W in CANDIDATE_WARPS:
+    for G in _candidates(S):
+        for W in (CANDIDATE_WARPS if G <= 32 else (8,)):
             b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT),
                       np.tile(net.E_constant(), (n_chains, 1)), np.tile(net.electrodes[:, 3], (n_chains, 1)),
                       np.tile(net.occupation.astype(np.uint8), (n_chains, 1)), np.full(n_chains, 2 * hops),
-                      seed=seed, lanes=G, warps_per_block=W, dev=dev)
+                      seed=seed, lanes=G, warps_per_block=W, dev=dev, pair_mode=pair_mode)
             b.launch(1024)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
             b.launch(hops)
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t0
-            rate = n_chains * hops / dt
+            e1.record()
+            e1.synchronize()
+            rate = n_chains * hops / (e0.elapsed_time(e1) * 1e-3)
             table.append((G, W, rate))
             if verbose:
                 print(f"S={S} C={n_chains} G={G} W={W}: {rate:.3e} hops/s")
@@ -100,18 +112,22 @@ def tune_size_class(S, n_chains, hops=4096, seed=0, dev=None, verbose=False):
                 table=[list(map(float, r)) for r in table])
 
 
-def choose(S_values, n_chains, dev=None, tune=True):
-    """Per-size-class lanes for a workload: a callable S -> G (cached)."""
+def choose(S_values, n_chains=None, dev=None, tune=True, pair_mode="table", max_tune_chains=8192):
+    """Per-size-class lanes for a workload: a callable S -> G.  Each size
+    class is tuned with its own chain count (from S_values, capped at
+    max_tune_chains), or n_chains when given; results are cached."""
     import torch
     gpu = torch.cuda.get_device_name(dev) if torch.cuda.is_available() else "none"
-    classes = sorted({size_class(int(s)) for s in np.atleast_1d(S_values)})
+    S_values = np.atleast_1d(np.asarray(S_values, dtype=np.int64))
+    classes, counts = np.unique([size_class(int(s)) for s in S_values], return_counts=True)
     with _LOCK:
         cache = _load()
         picked = {}
-        for sc in classes:
-            k = _key(gpu, sc, n_chains)
+        for sc, cnt in zip(classes.tolist(), counts.tolist()):
+            nc = int(min(n_chains if n_chains else cnt, max_tune_chains))
+            k = _key(gpu, sc, nc) + f"|{pair_mode}"
             if k not in cache and tune:
-                cache[k] = tune_size_class(sc, n_chains, dev=dev)
+                cache[k] = tune_size_class(sc, nc, dev=dev, pair_mode=pair_mode)
                 _save(cache)
             picked[sc] = cache[k]["G"] if k in cache else None
     from .engine import default_lanes
@@ -119,4 +135,5 @@ def choose(S_values, n_chains, dev=None, tune=True):
     def lanes(S):
         g = picked.get(size_class(S))
         return g if g else default_lanes(S)
+    lanes.picked = picked
     return lanes

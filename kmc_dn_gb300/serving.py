@@ -13,11 +13,11 @@ seed.  The server
   chains are superposed on the device (``kmc_site_energies``);
 * admits waiting requests, least work first (chains x hops x pairs per
   hop), while their chain state fits the device memory budget; long
-  requests (more than ``short_hops`` hops) may hold at most
-  ``max_active_long_chains`` resident chains -- about what fills the
-  device's chain slots -- so a short request is admitted on arrival
-  instead of queueing behind minutes of long work; admitted state stays
-  resident until the request is done;
+  requests (more than ``short_hops`` hops) may occupy at most
+  ``long_thread_share`` of the device's resident-thread slots (chains x
+  threads per chain), so a short request is admitted on arrival and finds
+  room on the SMs instead of queueing behind minutes of long work;
+  admitted state stays resident until the request is done;
 * runs every admitted request in quanta of hops on a CUDA stream of its own
   (pooled and reused), so requests that arrive while others run are started
   at once, their launches overlap on the device, and reading a finished
@@ -85,7 +85,8 @@ class Server:
     short_lanes_factor: short requests run with this many times the default
                     threads per chain (lower latency, lower throughput)
     short_hops:     requests with at most this many hops are short
-    max_active_long_chains: resident chains of long requests (default 8192)
+    long_thread_share: fraction of the device's resident-thread slots that
+                    long requests may hold (default 0.75)
     max_active_chains:      resident chains in all
     mem_budget:     bytes of chain state admitted at once (default: a
                     quarter of the free device memory at start)
@@ -95,7 +96,7 @@ class Server:
 
     def __init__(self, networks, *, quantum=4096, mem_budget=None,
                  pair_mode="positions", lanes=None, dev=None, short_hops=20000,
-                 max_active_chains=16384, max_active_long_chains=8192, quantum_long=_REANCHOR,
+                 max_active_chains=16384, long_thread_share=0.75, quantum_long=_REANCHOR,
                  short_lanes_factor=4):
         if quantum % _REANCHOR or quantum_long % _REANCHOR or quantum_long <= 0:
             raise ValueError("quantum and quantum_long must be multiples of the re-anchor period (1024)")
@@ -112,9 +113,12 @@ class Server:
         self.mem_budget = int(mem_budget if mem_budget is not None else free // 4)
         self.mem_used = 0
         self.max_active_chains = int(max_active_chains)
-        self.max_active_long_chains = int(max_active_long_chains)
+        props = torch.cuda.get_device_properties(self.dev)
+        self.long_thread_budget = int(long_thread_share * props.multi_processor_count
+                                      * props.max_threads_per_multi_processor)
         self.active_chains = 0
         self.active_long_chains = 0
+        self.active_long_threads = 0
         lo, hi = torch.cuda.Stream.priority_range()
         # every active request owns a stream (no request waits behind another's
         # launches); finished requests return theirs to a pool per priority
@@ -211,6 +215,13 @@ class Server:
         net = self.networks[req.geometry]
         return min(512, default_lanes(net.N + net.P) * self.short_lanes_factor)
 
+    def _threads(self, req):
+        """Resident threads the request's chains occupy."""
+        from .engine import default_lanes
+        net = self.networks[req.geometry]
+        G = self._lanes(req) or default_lanes(net.N + net.P)
+        return req.voltages.shape[0] * G
+
     def _admit(self):
         if not self.queue:
             return
@@ -223,7 +234,8 @@ class Server:
             if self.active:
                 if self.mem_used + need > self.mem_budget or self.active_chains + n > self.max_active_chains:
                     break
-                if long_ and self.active_long_chains + n > self.max_active_long_chains:
+                if long_ and self.active_long_threads > 0 and \
+                        self.active_long_threads + self._threads(req) > self.long_thread_budget:
                     continue        # a shorter request further down may still fit
             self.queue.remove(req)
             self._prepare(req, need)
@@ -250,6 +262,7 @@ class Server:
         self.active_chains += n
         if req.hops > self.short_hops:
             self.active_long_chains += n
+            self.active_long_threads += self._threads(req)
         self.active.append(req)
 
     def _launch_ready(self):
@@ -286,6 +299,7 @@ class Server:
                 self.active_chains -= req.voltages.shape[0]
                 if req.hops > self.short_hops:
                     self.active_long_chains -= req.voltages.shape[0]
+                    self.active_long_threads -= self._threads(req)
                 req.batch = None
                 self._free_streams[req.hops <= self.short_hops].append(req.stream)
                 self.finished.append(req)

@@ -95,3 +95,12 @@ def test_replicas_over_two_gloo_ranks(tmp_path):
     np.testing.assert_array_equal(np.array(r[0]["V"] + r[1]["V"]), V)
     for k in range(2):
         assert r[k]["ms"] == 20.0 and r[k]["hops"] == 3000
+
+
+def test_autotune_size_classes_and_candidates():
+    from kmc_dn_gb300 import autotune
+    assert autotune.size_class(20) == 24 and autotune.size_class(38) == 48 and autotune.size_class(212) == 256
+    assert autotune.size_class(5000) == 2048
+    assert autotune._candidates(38) == [4, 8, 16, 32]
+    assert autotune._candidates(212) == [4, 8, 16, 32, 64, 128, 256, 512]
+    assert autotune._candidates(1008) == [64, 128, 256, 512]

@@ -68,10 +68,11 @@ def test_latency_summary(engine_lib):
     assert s["all"]["p99_ms"] >= s["all"]["p50_ms"] > 0
 
 
-def test_short_requests_bypass_the_long_chain_cap(engine_lib):
-    """Long requests hold at most max_active_long_chains resident chains; a
+def test_short_requests_bypass_the_long_request_budget(engine_lib):
+    """Long requests hold at most their share of the device's thread slots; a
     short request is admitted beside them at once."""
-    srv, nets = _server(quantum=2048, max_active_long_chains=64, short_hops=4096)
+    srv, nets = _server(quantum=2048, short_hops=4096)
+    srv.long_thread_budget = 64 * 16        # room for one 64-chain request of 16 lanes
     longs = [srv.submit(0, np.zeros((64, 8)), 8192, seed=i) for i in range(2)]
     short = srv.submit(0, np.zeros((16, 8)), 2048, seed=9)
     with srv.lock:
