@@ -89,6 +89,7 @@ def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pai
                                  I_0=50.0, cells=40)
     spec = TableSpec.from_network(net) if pair_mode == "positions" else \
         TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    from ._native import KmcError
     table = []
     for G in _candidates(S):
         for W in (CANDIDATE_WARPS if G <= 32 else (8,)):
@@ -96,7 +97,10 @@ def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pai
                       np.tile(net.E_constant(), (n_chains, 1)), np.tile(net.electrodes[:, 3], (n_chains, 1)),
                       np.tile(net.occupation.astype(np.uint8), (n_chains, 1)), np.full(n_chains, 2 * hops),
                       seed=seed, lanes=G, warps_per_block=W, dev=dev, pair_mode=pair_mode)
-            b.launch(1024)
+            try:
+                b.launch(1024)
+            except KmcError:            # the shape does not fit (shared memory): not a candidate
+                continue
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()

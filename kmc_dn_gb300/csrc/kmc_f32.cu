@@ -647,7 +647,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             u_ev = grp.bcast2(rnd_u, ri);
         }
         if (sm.rates) grp.sync();   // stored rates visible to the whole group
-        // ---- FP64 scan of the per-thread sums ----
+        // ---- double-float scan of the per-thread sums ----
         F2 excl, tot;
         const F2 incl = grp.scan_df(lsum, excl, tot);
         if (!(tot.hi > 0.0f) || !(tot.hi <= 3.0e38f)) { status = KMC_ERR_NONFINITE; break; }
