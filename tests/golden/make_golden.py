@@ -217,14 +217,37 @@ def small_cases(hops):
     return cases
 
 
+def time_reference(ref_path, hops):
+    """Wall time of one call of the reference's _simulate_discrete_record
+    (kmc_dopant_networks.py:33-135, numba stubbed out, numpy's own random
+    generator) for `hops` hops on the benchmark network."""
+    ref = load_reference(ref_path)
+    net = workloads.plain_network(0)
+    S = net.S
+    np.random.seed(1)
+    t0 = time.perf_counter()
+    ref._simulate_discrete_record(net.N, net.P, net.nu, net.kT, net.I_0, net.R, 0,
+                                  net.occupation.astype(bool).copy(), net.distances, net.E_constant(),
+                                  net.site_energies(), net.transitions_constant, np.zeros((S, S)),
+                                  np.zeros(S * S), np.zeros(net.P, dtype=np.int64), hops, record=False)
+    dt = time.perf_counter() - t0
+    print(f"reference _simulate_discrete_record (plain Python, 1 core): {hops} hops in {dt:.1f} s "
+          f"= {hops / dt:.1f} hops/s")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("KMC_DN_REFERENCE", "/root/reference"))
     ap.add_argument("--quick", action="store_true", help="short runs only")
     ap.add_argument("--long-hops", type=int, default=100_000)
     ap.add_argument("--only", default=None)
+    ap.add_argument("--time-reference", type=int, default=0, metavar="HOPS",
+                    help="only time the reference's own hop loop (plain Python, one core) for "
+                         "HOPS hops on the N=30, P=8 benchmark network and print hops/s")
     args = ap.parse_args()
     ref = args.reference
+    if args.time_reference:
+        return time_reference(ref, args.time_reference)
     long_hops = 2000 if args.quick else args.long_hops
 
     cases = [fixture_case(ref, "thesis_indrek/tests/rnd_min_max/test0.kmc", 11, long_hops),
