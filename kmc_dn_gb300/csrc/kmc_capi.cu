@@ -41,11 +41,11 @@ int ok()
     return KMC_OK;
 }
 
-// Automatic lanes-per-chain: enough lanes that a chain's pair loop stays
-// short, few enough that per-hop group overhead (scans, FP64 compare) is
-// shared by several chains per warp.
-// Threads per chain by network size, as measured best on GB300: warp
-// slices for small networks, whole blocks for large ones.
+// Automatic lanes per chain (threads per chain) by network size, as
+// measured best on GB300: enough lanes that a chain's pair walk stays short,
+// few enough that the per-hop group work (scan, search, list rebuild) is
+// shared by several chains per warp for small networks; whole blocks for
+// large ones.
 static int auto_lanes(int S)
 {
     if (S <= 48) return 16;
