@@ -523,7 +523,12 @@ def bench_large(args):
     hops = args.hops if args.hops != HOPS else 100_000
     nets = [workloads.large_network(seed=1000 + i) for i in range(n)]
     specs = [TableSpec.from_network(net) for net in nets]
-    lanes = args.lanes or 256
+    lanes, tune_s = args.lanes or 256, 0.0
+    if not args.lanes and not args.no_autotune:
+        from kmc_dn_gb300 import autotune
+        t0 = time.perf_counter()
+        lanes = autotune.choose([s.S for s in specs], pair_mode="positions")(specs[0].S)
+        tune_s = time.perf_counter() - t0
     b = Batch(specs, np.arange(n), [1.0] * n, [net.E_constant() for net in nets],
               [net.electrodes[:, 3] for net in nets], [net.occupation.astype(np.uint8) for net in nets],
               [10**12] * n, seed=args.seed + 9, pair_mode="positions", lanes=lanes)
@@ -548,6 +553,7 @@ def bench_large(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "large networks: 256 chains, own N=1000 M=100 networks, 8 electrodes",
                        "n_chains": n, "hops_per_chain_timed": hops, "lanes_per_chain": lanes,
+                       "lanes": "autotuned" if tune_s else "fixed", "autotune_s": tune_s,
                        "pair_mode": "positions"},
             "roofline": {"bound": "sfu", "achieved": pairs / dt / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gexp/s", "frac": pairs / dt / peak.value,
