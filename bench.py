@@ -137,8 +137,12 @@ def accuracy_of(cases, dev, replicas=32, hops=300_000, seed=0, pair_mode="table"
 
     ``cases``: (network, voltages) pairs; each runs ``replicas`` independent
     times on both.  Per current: the z-score of the mean difference and,
-    where the standard error resolves it (below 0.25 % of the current), the
-    relative difference."""
+    where the standard error resolves it (below 1/3 % of the current, so that
+    a 1 % difference would stand at 3 sigma), the relative difference.  Per
+    site the time-averaged occupation likewise (z-score and absolute
+    difference; both kernels credit occupancy after the hop, the numba
+    convention)."""
+    from kmc_dn_gb300 import _native
     from kmc_dn_gb300.engine import Batch, TableSpec, simulate_f64_many
     rows = [c for c in range(len(cases)) for _ in range(replicas)]
     specs = [TableSpec.from_network(net) if pair_mode == "positions" else
@@ -147,16 +151,17 @@ def accuracy_of(cases, dev, replicas=32, hops=300_000, seed=0, pair_mode="table"
     b = Batch(specs, np.array(rows, np.int32), [cases[c][0].kT for c in rows],
               [cases[c][0].E_constant(cases[c][1]) for c in rows], [cases[c][1] for c in rows],
               [cases[c][0].occupation.astype(np.uint8) for c in rows], np.full(len(rows), hops),
-              streams=np.arange(len(rows)) + 10_000_000, seed=seed + 101, dev=dev, pair_mode=pair_mode)
+              streams=np.arange(len(rows)) + 10_000_000, seed=seed + 101, dev=dev, pair_mode=pair_mode,
+              record=_native.RECORD_NUMBA)
     r32 = b.run().results()
     assert np.all(r32["status"] == 0)
     chains = [dict(N=n.N, P=n.P, nu=n.nu, kT=n.kT, I_0=n.I_0, R=n.R, occupation=n.occupation,
                    distances=n.distances, E_constant=n.E_constant(v), site_energies=n.site_energies(v),
                    transitions_constant=n.transitions_constant) for n, v in (cases[c] for c in rows)]
-    t64, eo64, st64 = simulate_f64_many(chains, hops, [seed * 7919 + 13 + i for i in range(len(rows))], dev=dev,
-                                        n_streams=128)
+    t64, eo64, st64, oit64 = simulate_f64_many(chains, hops, [seed * 7919 + 13 + i for i in range(len(rows))],
+                                               dev=dev, n_streams=128, record=True)
     assert np.all(st64 == 0)
-    zs, rels, res, rse = [], [], [], []
+    zs, rels, res, rse, ozs, odiff = [], [], [], [], [], []
     for c in range(len(cases)):
         idx = [i for i, rc in enumerate(rows) if rc == c]
         I32 = np.stack([r32["electrode_occupation"][i] / r32["time"][i] for i in idx])
@@ -167,13 +172,23 @@ def accuracy_of(cases, dev, replicas=32, hops=300_000, seed=0, pair_mode="table"
         rels.append(np.abs(m32 - m64) / np.maximum(np.abs(m64), 1e-300))
         res.append(se < np.abs(m64) / 300.0)
         rse.append(se / np.maximum(np.abs(m64), 1e-300))
+        O32 = np.stack([r32["occ_time"][i] / r32["time"][i] for i in idx])
+        O64 = np.stack([oit64[i] / t64[i] for i in idx])
+        osd = np.sqrt(O32.var(0, ddof=1) / replicas + O64.var(0, ddof=1) / replicas)
+        od = np.abs(O32.mean(0) - O64.mean(0))
+        ozs.append(od / np.maximum(osd, 1e-12))
+        odiff.append(od)
     z, rel, resolved = np.concatenate(zs), np.concatenate(rels), np.concatenate(res)
     rse = np.concatenate(rse)
+    oz, od = np.concatenate(ozs), np.concatenate(odiff)
     return {"currents": int(z.size), "chains": len(cases), "replicas": replicas, "hops": hops,
             "max_abs_z": float(z.max()), "frac_within_3sigma": float(np.mean(z <= 3.0)),
             "median_rel_se": float(np.median(rse)), "resolved_currents": int(resolved.sum()),
             "max_rel_err_resolved": float(rel[resolved].max()) if resolved.any() else None,
-            "frac_resolved_within_1pct": float(np.mean(rel[resolved] <= 0.01)) if resolved.any() else None}
+            "frac_resolved_within_1pct": float(np.mean(rel[resolved] <= 0.01)) if resolved.any() else None,
+            "occupancies": int(oz.size), "occupancy_max_abs_z": float(oz.max()),
+            "occupancy_frac_within_3sigma": float(np.mean(oz <= 3.0)),
+            "occupancy_max_abs_diff": float(od.max())}
 
 
 def accuracy_sample(net, V, dev, n_chains=4, replicas=32, hops=300_000, seed=0):

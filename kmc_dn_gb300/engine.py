@@ -100,13 +100,14 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     return out
 
 
-def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None):
+def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None, record=False):
     """Run independent FP64 chains concurrently (one kernel launch per chain,
     spread over ``n_streams`` CUDA streams), for FP64 reference statistics.
 
     ``chains``: list of dicts with N, P, nu, kT, I_0, R, occupation,
     distances, E_constant, site_energies, transitions_constant.  Returns
-    (time[C], electrode_occupation[C][P], status[C])."""
+    (time[C], electrode_occupation[C][P], status[C]) and, with ``record``,
+    a fourth list: occupations_in_time[C][N] (numba convention)."""
     d = device(dev)
     f64 = torch.float64
     L = lib()
@@ -126,18 +127,22 @@ def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None):
             eo = torch.zeros(max(P, 1), dtype=torch.int64, device=d)
             t_out = torch.zeros(1, dtype=f64, device=d)
             s_out = torch.zeros(1, dtype=torch.int32, device=d)
+            tr = torch.zeros(S * S, dtype=f64, device=d) if record else None
+            oit = torch.zeros(max(N, 1), dtype=f64, device=d) if record else None
             wsb = L.kmc_simulate_f64_workspace_size(S)
             ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
         check(L.kmc_simulate_f64(N, P, float(ch["nu"]), float(ch["kT"]), float(ch["I_0"]), float(ch["R"]),
-                                 _ptr(occ), _ptr(dist), _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), int(hops), 0,
-                                 None, None, None, int(seed) & (2**64 - 1), None, _ptr(t_out), _ptr(s_out),
-                                 _ptr(ws), wsb, _stream_handle(st)))
-        keep.append((occ, dist, tc, ec, se, ws))
-        outs.append((t_out, eo, s_out, P))
+                                 _ptr(occ), _ptr(dist), _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), int(hops),
+                                 int(bool(record)), _ptr(tr), _ptr(oit), None, int(seed) & (2**64 - 1), None,
+                                 _ptr(t_out), _ptr(s_out), _ptr(ws), wsb, _stream_handle(st)))
+        keep.append((occ, dist, tc, ec, se, ws, tr))
+        outs.append((t_out, eo, s_out, P, oit, N))
     torch.cuda.synchronize(d)
-    times = np.array([float(t.item()) for t, _, _, _ in outs])
-    eos = [e.cpu().numpy()[:P] for _, e, _, P in outs]
-    status = np.array([int(s.item()) for _, _, s, _ in outs])
+    times = np.array([float(o[0].item()) for o in outs])
+    eos = [o[1].cpu().numpy()[:o[3]] for o in outs]
+    status = np.array([int(o[2].item()) for o in outs])
+    if record:
+        return times, eos, status, [o[4].cpu().numpy()[:o[5]] for o in outs]
     return times, eos, status
 
 
