@@ -4,6 +4,8 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
+
 from conftest import REPO
 
 
@@ -88,3 +90,16 @@ def test_engine_handle_rejects_bad_arguments_without_gpu(engine_lib):
     assert "NULL engine" in last_error()[1]
     assert L.kmc_engine_read(None, None, None, None, None, None, None, None) == KMC_ERR_INVALID
     L.kmc_engine_destroy(None)          # a no-op
+
+
+def test_empty_batches_are_a_no_op_without_gpu(engine_lib):
+    """Zero chains: the host entry points return KMC_OK before touching the
+    device (the reference's parallelSimulations returns at once too)."""
+    from kmc_dn_gb300._native import KMC_OK, lib
+    L = lib()
+    one = np.ones(1)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    gN, gP, off = np.array([4], np.int32), np.array([2], np.int32), np.zeros(1, np.int64)
+    rc = L.kmc_run_batch_host(1, p(gN), p(gP), p(one), p(one), p(one), p(off), p(np.ones(36)), p(np.ones(36)), 0,
+                              None, None, None, None, None, None, 0, 0, None, None, None)
+    assert rc == KMC_OK

@@ -281,3 +281,49 @@ def test_positions_mode_rejects_inconsistent_tables(engine_lib):
     with pytest.raises(ValueError):
         Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]],
               [net.occupation.astype(np.uint8)], [10], pair_mode="positions")
+
+
+@pytest.mark.parametrize("pair_mode", ["positions", "table"])
+def test_largest_network_runs(engine_lib, pair_mode):
+    """S = 2048 sites (the engine's limit: pair indices stay below 2^22) with
+    64 electrodes (the electrode limit), block groups of 512."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    N, P = 2048 - 64, 64
+    rng = np.random.Generator(np.random.PCG64(5))
+    L = float(np.sqrt(N / workloads.DENSITY))
+    net = workloads.make_network(rng, N, N // 10, L, L, workloads.perimeter_electrodes(L, P),
+                                 voltages=rng.uniform(-1, 1, P), I_0=50.0)
+    spec = TableSpec.from_network(net) if pair_mode == "positions" else \
+        TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    b = Batch([spec], [0, 0], [1.0, 1.0], [net.E_constant()] * 2, [net.electrodes[:, 3]] * 2,
+              [net.occupation.astype(np.uint8)] * 2, [300, 300], lanes=512, pair_mode=pair_mode, seed=3)
+    r = b.run().results()
+    assert (r["status"] == 0).all() and (r["hops_done"] == 300).all() and (r["time"] > 0).all()
+    # holes are conserved up to what the electrodes absorbed
+    for c in range(2):
+        assert int(r["occupation"][c].sum()) - int(net.occupation.sum()) == -int(r["electrode_occupation"][c].sum())
+
+
+def test_sizes_beyond_the_limits_are_rejected(engine_lib):
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300._native import KMC_ERR_INVALID, KmcError
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    # 2049 sites: refused before any launch
+    N, P = 2049 - 8, 8
+    S = N + P
+    d = np.ones((S, S))
+    np.fill_diagonal(d, 0.0)
+    spec = TableSpec(N, P, 1.0, 1.0, 1.0, d, np.zeros((S, S)))
+    with pytest.raises(KmcError):
+        Batch([spec], [0], [1.0], [np.zeros(N)], [np.zeros(P)], [np.zeros(N, np.uint8)], [10],
+              lanes=512).run()
+    # 65 electrodes: the chain reports an invalid status
+    rng = np.random.Generator(np.random.PCG64(1))
+    L = float(np.sqrt(100 / workloads.DENSITY))
+    net = workloads.make_network(rng, 100, 10, L, L, workloads.perimeter_electrodes(L, 65),
+                                 voltages=np.zeros(65), I_0=50.0, cells=40)
+    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    r = Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]], [net.occupation.astype(np.uint8)],
+              [10], lanes=128).run().results()
+    assert r["status"][0] == KMC_ERR_INVALID
