@@ -307,7 +307,7 @@ def test_largest_network_runs(engine_lib, pair_mode):
 
 def test_sizes_beyond_the_limits_are_rejected(engine_lib):
     from kmc_dn_gb300 import workloads
-    from kmc_dn_gb300._native import KMC_ERR_INVALID, KmcError
+    from kmc_dn_gb300._native import KmcError
     from kmc_dn_gb300.engine import Batch, TableSpec
     # 2049 sites: refused before any launch
     N, P = 2049 - 8, 8
@@ -318,12 +318,13 @@ def test_sizes_beyond_the_limits_are_rejected(engine_lib):
     with pytest.raises(KmcError):
         Batch([spec], [0], [1.0], [np.zeros(N)], [np.zeros(P)], [np.zeros(N, np.uint8)], [10],
               lanes=512).run()
-    # 65 electrodes: the chain reports an invalid status
+    # 65 electrodes: refused by the host before any launch (the kernel would
+    # also mark the chain KMC_ERR_INVALID)
     rng = np.random.Generator(np.random.PCG64(1))
     L = float(np.sqrt(100 / workloads.DENSITY))
     net = workloads.make_network(rng, 100, 10, L, L, workloads.perimeter_electrodes(L, 65),
                                  voltages=np.zeros(65), I_0=50.0, cells=40)
     spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
-    r = Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]], [net.occupation.astype(np.uint8)],
-              [10], lanes=128).run().results()
-    assert r["status"][0] == KMC_ERR_INVALID
+    with pytest.raises(ValueError, match="at most 64 electrodes"):
+        Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]], [net.occupation.astype(np.uint8)],
+              [10], lanes=128)
