@@ -198,6 +198,12 @@ typedef struct kmc_batch {
     const int64_t *tab_pos_off;     /* [n_tables] offset in floats into tab_pos*/
     const float *tab_coef;          /* [n_tables*4]: -2*log2(e)/ab,
                                        log2(nu*nu), I_0*R, 0                   */
+    /* wall-clock budget of one launch per chain, checked with the cancel word
+     * every 1024 hops (not before the first 1024 of a launch); a chain that
+     * overruns stops with KMC_ERR_TIMEOUT at a multiple of 1024 hops, its
+     * state consistent, and a later launch resumes it as if uninterrupted.
+     * 0: none */
+    int64_t time_budget_ns;
 } kmc_batch;
 
 /*
@@ -351,6 +357,13 @@ typedef struct kmc_mf_batch {
     int32_t *status;                /* [n_chains] or NULL                      */
     int64_t *iterations_done;       /* [n_chains] or NULL                      */
 } kmc_mf_batch;
+
+/* A cancel word the host can set while kernels run (pinned, mapped host
+ * memory): *host_word = 1 makes every chain of a launch that carries
+ * device_word as kmc_batch.cancel stop at its next 1024-hop check with
+ * KMC_ERR_CANCELLED, state consistent. */
+int kmc_cancel_word_create(int32_t **host_word, int32_t **device_word);
+void kmc_cancel_word_destroy(int32_t *host_word);
 
 /* Largest S a chain may have for the given rate precision (its tables and
  * rates stay in one block's shared memory). */

@@ -59,6 +59,7 @@ class KmcBatch(C.Structure):
         ("warps_per_block", _i32), ("max_hops_per_launch", _i64), ("seed", _u64),
         ("replay", _vp), ("replay_off", _vp), ("cancel", _vp),
         ("pair_mode", _i32), ("tab_pos", _vp), ("tab_pos_off", _vp), ("tab_coef", _vp),
+        ("time_budget_ns", _i64),
     ]
 
 
@@ -92,6 +93,8 @@ _SIGS = {
     "kmc_measure_ex2_rate": (C.c_int, [C.POINTER(_f64)]),
     "kmc_run_batch_host": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _u64, _i32, _vp, _vp, _vp]),
+    "kmc_cancel_word_create": (C.c_int, [_vp, _vp]),
+    "kmc_cancel_word_destroy": (None, [_vp]),
     "kmc_engine_create": (C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp,
                                     _vp, _vp, _vp, _u64, _i32, _i32, _vp]),
     "kmc_engine_run": (C.c_int, [_vp, _i64]),

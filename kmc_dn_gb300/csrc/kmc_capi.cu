@@ -461,6 +461,30 @@ int kmc_run_batch_host(int32_t n_geoms, const int32_t *geom_N, const int32_t *ge
     return host_run(h);
 }
 
+int kmc_cancel_word_create(int32_t **host_word, int32_t **device_word)
+{
+    if (!host_word || !device_word) return fail(KMC_ERR_INVALID, "kmc_cancel_word_create: NULL argument");
+    *host_word = nullptr;
+    *device_word = nullptr;
+    void *h = nullptr, *d = nullptr;
+    cudaError_t e = cudaHostAlloc(&h, sizeof(int32_t), cudaHostAllocMapped);
+    if (e != cudaSuccess) return fail_cuda(e, "kmc_cancel_word_create: cudaHostAlloc");
+    *static_cast<volatile int32_t *>(h) = 0;
+    e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(h);
+        return fail_cuda(e, "kmc_cancel_word_create: cudaHostGetDevicePointer");
+    }
+    *host_word = static_cast<int32_t *>(h);
+    *device_word = static_cast<int32_t *>(d);
+    return KMC_OK;
+}
+
+void kmc_cancel_word_destroy(int32_t *host_word)
+{
+    if (host_word) cudaFreeHost(host_word);
+}
+
 int kmc_engine_create(kmc_engine **engine, int32_t n_geoms, const int32_t *geom_N, const int32_t *geom_P,
                       const double *geom_nu, const double *geom_I0, const double *geom_R,
                       const int64_t *geom_pair_off, const double *distances,

@@ -76,6 +76,14 @@ __device__ __forceinline__ float rcp_approx(float x)
     return y;
 }
 
+// Nanosecond wall clock of the GPU (PTX %globaltimer).
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ float rsqrt_approx(float x)
 {
     float y;
@@ -497,6 +505,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 
     double t = B.time[c];    // the clock: FP64 (one add per hop, off the critical path)
     int64_t hop = hops_done0;
+    const uint64_t t_launch = B.time_budget_ns > 0 ? globaltimer_ns() : 0;
     const int64_t hop_end = hops_done0 + (todo > 0 ? todo : 0);
     int status = KMC_OK;
     unsigned long long npairs = 0;
@@ -556,9 +565,17 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
 
     while (hop < hop_end) {
-        if (B.cancel && (hop & 1023) == 0) {
-            const int stop = grp.bcast(g == 0 ? *B.cancel : 0, 0);
-            if (stop) { status = KMC_ERR_CANCELLED; break; }
+        if ((hop & 1023) == 0 && (B.cancel || (B.time_budget_ns > 0 && hop != hops_done0))) {
+            // the host's cancel word, then the launch's wall-clock budget
+            int stop = 0;
+            if (g == 0) {
+                if (B.cancel && *B.cancel) stop = KMC_ERR_CANCELLED;
+                else if (B.time_budget_ns > 0 && hop != hops_done0 &&
+                         static_cast<int64_t>(globaltimer_ns() - t_launch) > B.time_budget_ns)
+                    stop = KMC_ERR_TIMEOUT;
+            }
+            stop = grp.bcast(stop, 0);
+            if (stop) { status = stop; break; }
         }
         if (until_anchor == 0) {
             grp.sync();           // bit updates of the last hop are visible

@@ -28,7 +28,7 @@ from . import _native
 from ._native import check, lib
 
 __all__ = ["simulate_f64", "TableSpec", "TableSet", "Batch", "simulate_cuda", "simulate_go", "superpose",
-           "default_lanes", "make_work_lists", "device", "prune"]
+           "default_lanes", "make_work_lists", "device", "prune", "CancelWord", "simulate_f64_many"]
 
 
 def device(dev=None):
@@ -98,6 +98,41 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     if hop_log:
         out["hop_log"] = log.cpu().numpy()[: 2 * hops].reshape(hops, 2)
     return out
+
+
+class CancelWord:
+    """A flag the host sets while kernels run (pinned, mapped host memory,
+    kmc_cancel_word_create).  Give it to ``Batch.cancel``: after ``set()``
+    every chain of that batch's running and later launches stops at its next
+    1024-hop check with KMC_ERR_CANCELLED, its state consistent (``clear()``
+    and a further launch resume it as if uninterrupted)."""
+
+    def __init__(self):
+        h, d = C.c_void_p(), C.c_void_p()
+        check(lib().kmc_cancel_word_create(C.byref(h), C.byref(d)))
+        self._host = C.cast(h, C.POINTER(C.c_int32))
+        self._h = h
+        self.device = d.value
+
+    def set(self):
+        self._host[0] = 1
+
+    def clear(self):
+        self._host[0] = 0
+
+    def is_set(self):
+        return bool(self._host[0])
+
+    def close(self):
+        if self._h is not None:
+            lib().kmc_cancel_word_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None, record=False):
@@ -391,7 +426,8 @@ class Batch:
             roff = np.concatenate([[0], np.cumsum([r.shape[0] for r in rows])[:-1]]).astype(np.int64)
             self.replay = _dev(np.concatenate(rows), torch.float64, d)
             self.replay_off = _dev(roff, torch.int64, d)
-        self.cancel = None
+        self.cancel = None            # a CancelWord, or None
+        self.time_budget_ns = 0       # per launch and chain; 0: none
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
 
     # -- work lists --------------------------------------------------------
@@ -438,7 +474,8 @@ class Batch:
         if self.replay is not None:
             b.replay, b.replay_off = self.replay.data_ptr(), self.replay_off.data_ptr()
         if self.cancel is not None:
-            b.cancel = self.cancel
+            b.cancel = self.cancel.device
+        b.time_budget_ns = int(self.time_budget_ns)
         b.pair_mode = self.pair_mode
         if self.tab_pos is not None:
             b.tab_pos, b.tab_pos_off, b.tab_coef = (self.tab_pos.data_ptr(), self.tab_pos_off.data_ptr(),

@@ -47,7 +47,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .engine import Batch, TableSet, TableSpec, _REANCHOR, superpose
+from .engine import Batch, CancelWord, TableSet, TableSpec, _REANCHOR, superpose
 
 __all__ = ["Request", "Server", "latency_summary"]
 
@@ -68,6 +68,8 @@ class Request:
     stream: Optional[torch.cuda.Stream] = None
     bytes: int = 0
     started: bool = False
+    cancel_word: Optional[object] = None   # engine.CancelWord while the request is active
+    cancelled: bool = False
 
 
 def _request_bytes(n_chains, N, P):
@@ -147,11 +149,36 @@ class Server:
         V = np.asarray(voltages, np.float64)
         if V.ndim != 2 or V.shape[1] != self.networks[geometry].P:
             raise ValueError("voltages must be (n_chains, P) for the geometry")
+        if not np.isfinite(V).all():
+            # the hop loop, like the reference's, treats a NaN energy
+            # difference as downhill and would run on silently: refuse here
+            raise ValueError("voltages must be finite")
         req = Request(int(geometry), V, int(hops), int(seed), arrival=time.perf_counter())
         with self.cv:
             self.queue.append(req)
             self.cv.notify()
         return req
+
+    def cancel(self, req):
+        """Cancel a request: a waiting one is dropped, an active one stops
+        its chains at their next 1024-hop check (a host-mapped cancel word
+        its kernels poll) and is finished with what it has; either way its
+        future gets a result with ``cancelled`` True and the chains'
+        status (KMC_ERR_CANCELLED for the stopped ones)."""
+        with self.lock:
+            if req in self.queue:
+                self.queue.remove(req)
+                req.cancelled = True
+                req.done_at = time.perf_counter()
+                req.future.set_result(dict(cancelled=True, status=np.full(req.voltages.shape[0],
+                                                                          _native.KMC_ERR_CANCELLED, np.int32)))
+                return True
+            if any(r is req for r in self.active):
+                req.cancelled = True
+                if req.cancel_word is not None:
+                    req.cancel_word.set()
+                return True
+        return False
 
     def start(self):
         self._stop = False
@@ -256,6 +283,8 @@ class Server:
                               np.tile(net.occupation.astype(np.uint8), (n, 1)), np.full(n, req.hops),
                               seed=req.seed, lanes=self._lanes(req), dev=self.dev, E_constant_dev=ec,
                               el_energy_dev=ve, pair_mode=self.pair_mode)
+        req.cancel_word = CancelWord()
+        req.batch.cancel = req.cancel_word
         self.launches += 1
         req.bytes = need
         self.mem_used += need
@@ -268,7 +297,7 @@ class Server:
     def _launch_ready(self):
         # least remaining work first
         for req in sorted(self.active, key=lambda r: r.hops - r.launched_hops):
-            if req.launched_hops >= req.hops:
+            if req.launched_hops >= req.hops or req.cancelled:
                 continue
             if req.inflight is not None and not req.inflight.query():
                 continue
@@ -287,20 +316,25 @@ class Server:
     def _collect(self):
         still = []
         for req in self.active:
-            if req.launched_hops >= req.hops and req.inflight is not None and req.inflight.query():
+            finished = req.launched_hops >= req.hops or req.cancelled
+            if finished and (req.inflight is None or req.inflight.query()):
                 r = req.batch.results(stream=req.stream)
                 cur = np.array([e / t if t > 0 else np.full(len(e), np.nan)
                                 for e, t in zip(r["electrode_occupation"], r["time"])])
                 req.done_at = time.perf_counter()
                 self.hops_done += int(np.sum(r["hops_done"]))
                 out = dict(currents=cur, time=r["time"], electrode_occupation=np.array(r["electrode_occupation"]),
-                           status=r["status"], latency=req.done_at - req.arrival)
+                           status=r["status"], latency=req.done_at - req.arrival, cancelled=req.cancelled,
+                           hops_done=r["hops_done"])
                 self.mem_used -= req.bytes
                 self.active_chains -= req.voltages.shape[0]
                 if req.hops > self.short_hops:
                     self.active_long_chains -= req.voltages.shape[0]
                     self.active_long_threads -= self._threads(req)
                 req.batch = None
+                if req.cancel_word is not None:
+                    req.cancel_word.close()
+                    req.cancel_word = None
                 self._free_streams[req.hops <= self.short_hops].append(req.stream)
                 self.finished.append(req)
                 req.future.set_result(out)
