@@ -305,7 +305,11 @@ class Server:
             seg = min(q, req.hops - req.launched_hops)
             seg_launch = ((seg + _REANCHOR - 1) // _REANCHOR) * _REANCHOR
             with torch.cuda.stream(req.stream):
+                # an NVTX range per launch: profilers show which request ran when
+                torch.cuda.nvtx.range_push(f"kmc g{req.geometry} c{req.voltages.shape[0]} "
+                                           f"hops {req.launched_hops}+{seg}")
                 req.batch.launch(seg_launch, stream=req.stream)
+                torch.cuda.nvtx.range_pop()
                 self.launches += len(req.batch._bins)
                 ev = torch.cuda.Event()
                 ev.record(req.stream)
