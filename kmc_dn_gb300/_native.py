@@ -17,7 +17,9 @@ __all__ = ["lib", "check", "KmcError", "NativeLibraryError", "KmcBatch", "LIB_PA
            "EXPORTED", "KmcMfBatch", "MF_RATES_F64", "MF_RATES_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libkmc_dn_gb300.so")
+# KMC_DN_GB300_LIB selects another build of the same ABI (the debug-checks
+# library of kmc_dn_gb300/build.py --debug-checks)
+LIB_PATH = os.environ.get("KMC_DN_GB300_LIB", os.path.join(HERE, "libkmc_dn_gb300.so"))
 
 KMC_OK = 0
 KMC_ERR_INVALID = -1

@@ -19,6 +19,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libkmc_dn_gb300.so")
+# The same sources with -DKMC_DEBUG_CHECKS: the hop loop checks its decoded
+# pair and list indices and stops a chain with KMC_ERR_INVALID instead of
+# touching memory out of range (a stand-in for compute-sanitizer).
+DEBUG_LIB = os.path.join(HERE, "libkmc_dn_gb300_debug.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
@@ -35,24 +39,28 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
-def _stale():
-    if not os.path.exists(LIB):
+def _stale(lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = sources() + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
     deps.append(os.path.join(os.path.dirname(HERE), "include", "kmc_dn_gb300.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(p) > t for p in deps)
 
 
-def build(force=False, verbose=False, extra=()):
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OBJ, exist_ok=True)
+def build(force=False, verbose=False, extra=(), debug_checks=False):
+    lib = DEBUG_LIB if debug_checks else LIB
+    objdir = OBJ + ("_debug" if debug_checks else "")
+    if debug_checks:
+        extra = tuple(extra) + ("-DKMC_DEBUG_CHECKS",)
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(objdir, exist_ok=True)
     exe = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
         cmd = [exe, *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -63,16 +71,16 @@ def build(force=False, verbose=False, extra=()):
 
     with ThreadPoolExecutor(max_workers=len(sources())) as ex:
         objs = list(ex.map(compile_one, sources()))
-    tmp = LIB + f".tmp{os.getpid()}"
+    tmp = lib + f".tmp{os.getpid()}"
     cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
     v = "-v" in sys.argv
     extra = ("-Xptxas", "-v") if v else ()
-    print(build(force=True, verbose=v, extra=extra))
+    print(build(force=True, verbose=v, extra=extra, debug_checks="--debug-checks" in sys.argv))

@@ -55,6 +55,16 @@ namespace {
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr int kMaxElectrodes = 64;
+// Debug builds (-DKMC_DEBUG_CHECKS) check the hop loop's decoded pair and
+// list indices once per hop outside the pair walk; a violation stops the
+// chain with KMC_ERR_INVALID before the index is used.  Release builds
+// compile the checks away.
+#ifdef KMC_DEBUG_CHECKS
+#define KMC_DCHECK(cond) do { if (!(cond)) dbg_bad = 1; } while (0)
+#else
+#define KMC_DCHECK(cond) do { } while (0)
+#endif
+
 #ifndef KMC_PAIR_UNROLL
 #define KMC_PAIR_UNROLL 2
 #endif
@@ -419,6 +429,9 @@ struct ChainSmem {
     uint32_t *occw;  // [W]   occupancy bits
     int *eo;         // [kMaxElectrodes] electrode counters of this launch
     float *rates;    // [rate_words] this hop's pair rates, or nullptr (recompute)
+#ifdef KMC_DEBUG_CHECKS
+    int rate_cap;    // words of `rates`
+#endif
 };
 
 template <typename Rec>
@@ -450,6 +463,9 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_
     c.occw = reinterpret_cast<uint32_t *>(c.E + S);
     c.eo = reinterpret_cast<int *>(c.occw + (S + 31) / 32);
     c.rates = rate_words > 0 ? reinterpret_cast<float *>(base + chain_list_words<Rec>(S)) : nullptr;
+#ifdef KMC_DEBUG_CHECKS
+    c.rate_cap = rate_words;
+#endif
     return c;
 }
 
@@ -505,6 +521,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 
     double t = B.time[c];    // the clock: FP64 (one add per hop, off the critical path)
     int64_t hop = hops_done0;
+#ifdef KMC_DEBUG_CHECKS
+    int dbg_bad = 0;
+#endif
     const uint64_t t_launch = B.time_budget_ns > 0 ? globaltimer_ns() : 0;
     const int64_t hop_end = hops_done0 + (todo > 0 ? todo : 0);
     int status = KMC_OK;
@@ -605,6 +624,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             if (kb < ke) {
                 int row, col;
                 decode_pair(kb, h, A1, T1, T2, inv1, inv2, row, col);
+                KMC_DCHECK(ke <= A && row >= 0 && row < h + P && col >= 0 && col < (row < h ? T1 : T2));
+                KMC_DCHECK(!sm.rates || (M - 1) * G + g < sm.rate_cap);
                 bool sa = row < h;
                 int Tc = sa ? T1 : T2;
                 Rec sr = sm.src[row];
@@ -723,9 +744,18 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (chosen < 0) chosen = last_pos;
         if (chosen < 0) { status = KMC_ERR_NONFINITE; break; }
         int row, col;
+        KMC_DCHECK(chosen >= 0 && chosen < A && L >= 0 && L < G);
         decode_pair(chosen, h, A1, T1, T2, inv1, inv2, row, col);
+        KMC_DCHECK(row >= 0 && row < h + P && col >= 0 && col < (row < h ? T1 : T2));
+#ifdef KMC_DEBUG_CHECKS
+        if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
+#endif
         const int from = Pairs::kSiteInRec ? Pairs::site(sm.src[row]) : sm.src_id[row];
         const int to = Pairs::kSiteInRec ? Pairs::site(sm.tgt[col]) : sm.tgt_id[col];
+        KMC_DCHECK(from >= 0 && from < S && to >= 0 && to < S && from != to && (from < N || to < N));
+#ifdef KMC_DEBUG_CHECKS
+        if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
+#endif
         // ---- clock ----
         const float dt = e1 * __frcp_rn(tot.hi);
         const double t_before = t;
@@ -749,6 +779,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 const int below = cum + __popc(word & ((1u << (j & 31)) - 1u))
                                   - ((fa && from < j) ? 1 : 0) + ((tb && to < j) ? 1 : 0);
                 const bool occ_j = (j == to && tb) || (j != from && ((word >> (j & 31)) & 1u));
+#ifdef KMC_DEBUG_CHECKS
+                if (occ_j ? !(below >= 0 && below < h_new) : !(j - below >= 0 && j - below < z_new)) {
+                    dbg_bad = 1;        // skip the store: the chain stops after this hop
+                    continue;
+                }
+#endif
                 const Rec r = pairs.rec(j, cs * Ej);
                 if (occ_j) {
                     sm.src[below] = r;
@@ -784,6 +820,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         h = h_new;
         ++hop;
+#ifdef KMC_DEBUG_CHECKS
+        if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
+#endif
     }
     grp.sync();
 
