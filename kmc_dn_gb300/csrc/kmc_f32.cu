@@ -66,10 +66,11 @@ constexpr int kMaxElectrodes = 64;
 #endif
 
 #ifndef KMC_PAIR_UNROLL
-#define KMC_PAIR_UNROLL 2
+#define KMC_PAIR_UNROLL 4
 #endif
-// Unroll of the pair walk (two steps = four pairs in flight per thread):
-// measured 7 % faster than no unrolling on the N=30 ensemble, no spills.
+// Unroll of the pair walk (four steps = eight pairs in flight per thread):
+// on the N=30 ensemble 10 % faster than no unrolling and 5 % faster than two
+// steps; the large networks are insensitive to it.
 constexpr int kPairUnroll = KMC_PAIR_UNROLL;
 
 __device__ __forceinline__ float ex2_approx(float x)
@@ -444,11 +445,12 @@ __host__ __device__ __forceinline__ int chain_list_words(int S)
 }
 
 // Words to keep every pair rate of one hop: A(h) <= S^2/3 for any split of
-// S sites into acceptors and electrodes, plus one row of G for the
-// transposed layout.
+// S sites into acceptors and electrodes; the transposed layout (element i of
+// thread g at i*G + g, i < M) reaches G*M <= A + 2G - 1 with M rounded up to
+// odd.
 __host__ __device__ __forceinline__ int rate_buffer_words(int S, int G)
 {
-    return (((S * S) / 3 + 1 + G) + 3) & ~3;
+    return (((S * S) / 3 + 1 + 2 * G) + 3) & ~3;
 }
 
 template <typename Rec>
@@ -610,7 +612,15 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (A <= 0) { status = KMC_ERR_NONFINITE; break; }
         const float inv1 = T1 > 0 ? rcp_approx(static_cast<float>(T1)) : 0.0f;
         const float inv2 = T2 > 0 ? rcp_approx(static_cast<float>(T2)) : 0.0f;
-        const int M = (A + G - 1) / G;
+        // Run length per thread.  Block groups round it up to an odd number:
+        // thread g's run starts M records after thread g-1's, and with long
+        // rows (few row changes inside a run) an odd stride puts the threads'
+        // 8- or 16-byte record loads in distinct banks, where an even M made
+        // them collide up to 8-fold (30 % faster on N=1000 networks).  Warp
+        // slices walk short rows whose wrap scrambles the stride anyway; they
+        // keep ceil(A/G), measured 1.5 % faster there.  Trailing threads may
+        // get short or empty runs.
+        const int M = ((A + G - 1) / G) | (G >= 64 ? 1 : 0);
         float lsum = 0.0f;
         {
             // The thread walks its contiguous run of pairs in row-major order,
@@ -691,7 +701,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (!(tot.hi > 0.0f) || !(tot.hi <= 3.0e38f)) { status = KMC_ERR_NONFINITE; break; }
         const F2 target = df_mul(u_ev, tot);
         int L = grp.first(df_ge(incl, target));
-        if (L < 0) L = G - 1;
+        if (L < 0) L = (A - 1) / M;   // u*total rounded above the total: the last non-empty run
         const F2 baseL = grp.bcast2(excl, L);
         float rem = df_add(target, F2{-baseL.hi, -baseL.lo}).hi;
         // ---- find the event inside thread L's run ----
