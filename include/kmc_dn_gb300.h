@@ -242,6 +242,16 @@ int kmc_run_batch(const kmc_batch *batch, void *stream);
 /* Lanes-per-chain choices compiled into the engine: bit k set = G of 2^k. */
 int kmc_engine_lane_options(void);
 
+/* Per-phase SM-clock cycles of the FP32 engine's hop loop, summed over the
+ * chains of every launch since the last reset (thread 0 of each group):
+ * cycles[0..7] = loop checks, pair walk, uniforms, group scan and target,
+ * event search, clock, energy update and list rebuild, hop bookkeeping;
+ * cycles[8] = hops.  reset != 0 zeroes the counters after reading.  Only a
+ * library built with -DKMC_SECTION_CLOCKS (kmc_dn_gb300/build.py
+ * --section-clocks) counts; the release library returns KMC_ERR_INVALID.
+ * No reference counterpart (measurement support). */
+int kmc_section_clocks(uint64_t *cycles, int32_t reset);
+
 /* Measure the device's ex2 (SFU) throughput in ex2 results per second: the
  * roofline of the rate evaluation.  Synchronous, on the current device.  No
  * reference counterpart (measurement support). */

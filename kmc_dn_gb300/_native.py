@@ -17,8 +17,8 @@ __all__ = ["lib", "check", "KmcError", "NativeLibraryError", "KmcBatch", "LIB_PA
            "EXPORTED", "KmcMfBatch", "MF_RATES_F64", "MF_RATES_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# KMC_DN_GB300_LIB selects another build of the same ABI (the debug-checks
-# library of kmc_dn_gb300/build.py --debug-checks)
+# KMC_DN_GB300_LIB selects another build of the same ABI (the debug-checks or
+# section-clocks library of kmc_dn_gb300/build.py)
 LIB_PATH = os.environ.get("KMC_DN_GB300_LIB", os.path.join(HERE, "libkmc_dn_gb300.so"))
 
 KMC_OK = 0
@@ -93,6 +93,7 @@ _SIGS = {
     "kmc_run_batch": (C.c_int, [C.POINTER(KmcBatch), _vp]),
     "kmc_engine_lane_options": (C.c_int, []),
     "kmc_measure_ex2_rate": (C.c_int, [C.POINTER(_f64)]),
+    "kmc_section_clocks": (C.c_int, [_vp, _i32]),
     "kmc_run_batch_host": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _u64, _i32, _vp, _vp, _vp]),
     "kmc_cancel_word_create": (C.c_int, [_vp, _vp]),

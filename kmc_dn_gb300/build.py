@@ -23,6 +23,9 @@ LIB = os.path.join(HERE, "libkmc_dn_gb300.so")
 # pair and list indices and stops a chain with KMC_ERR_INVALID instead of
 # touching memory out of range (a stand-in for compute-sanitizer).
 DEBUG_LIB = os.path.join(HERE, "libkmc_dn_gb300_debug.so")
+# The same sources with -DKMC_SECTION_CLOCKS: the hop loop times its phases
+# with the SM clock (kmc_section_clocks; kmc_dn_gb300/section_clocks.py).
+CLOCKS_LIB = os.path.join(HERE, "libkmc_dn_gb300_clocks.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
@@ -49,11 +52,15 @@ def _stale(lib=LIB):
     return any(os.path.getmtime(p) > t for p in deps)
 
 
-def build(force=False, verbose=False, extra=(), debug_checks=False):
-    lib = DEBUG_LIB if debug_checks else LIB
-    objdir = OBJ + ("_debug" if debug_checks else "")
+def build(force=False, verbose=False, extra=(), debug_checks=False, section_clocks=False):
+    if debug_checks and section_clocks:
+        raise ValueError("build one of the debug-checks and section-clocks libraries at a time")
+    lib = DEBUG_LIB if debug_checks else CLOCKS_LIB if section_clocks else LIB
+    objdir = OBJ + ("_debug" if debug_checks else "_clocks" if section_clocks else "")
     if debug_checks:
         extra = tuple(extra) + ("-DKMC_DEBUG_CHECKS",)
+    if section_clocks:
+        extra = tuple(extra) + ("-DKMC_SECTION_CLOCKS",)
     if not force and not _stale(lib):
         return lib
     os.makedirs(objdir, exist_ok=True)
@@ -83,4 +90,5 @@ def build(force=False, verbose=False, extra=(), debug_checks=False):
 if __name__ == "__main__":
     v = "-v" in sys.argv
     extra = ("-Xptxas", "-v") if v else ()
-    print(build(force=True, verbose=v, extra=extra, debug_checks="--debug-checks" in sys.argv))
+    print(build(force=True, verbose=v, extra=extra, debug_checks="--debug-checks" in sys.argv,
+                section_clocks="--section-clocks" in sys.argv))

@@ -384,6 +384,11 @@ int kmc_engine_lane_options(void)
     return (1 << 2) | (1 << 3) | (1 << 4) | (1 << 5) | (1 << 6) | (1 << 7) | (1 << 8) | (1 << 9);
 }
 
+int kmc_section_clocks(uint64_t *cycles, int32_t reset)
+{
+    return kmc::section_clocks(cycles, reset);
+}
+
 size_t kmc_simulate_f64_workspace_size(int32_t n_sites)
 {
     return n_sites > 0 ? f64_workspace_size(n_sites) : 0;

@@ -65,6 +65,23 @@ constexpr int kMaxElectrodes = 64;
 #define KMC_DCHECK(cond) do { } while (0)
 #endif
 
+// Section-clock builds (-DKMC_SECTION_CLOCKS) time the phases of every hop
+// with the SM clock; the group's thread 0 adds its per-phase cycle counts and
+// hop count to kSectionSlots device counters at the end of each launch
+// (kmc_section_clocks reads them).  Release builds compile them away.
+constexpr int kSections = 8;   // top, pairs, uniforms, scan, search, clock, rebuild, update
+#ifdef KMC_SECTION_CLOCKS
+__device__ unsigned long long g_section_clocks[kSections + 1];
+#define KMC_SECTION(k)                                                   \
+    do {                                                                 \
+        const uint32_t t_ = static_cast<uint32_t>(clock());              \
+        sec_cycles[k] += t_ - sec_last;                                  \
+        sec_last = t_;                                                   \
+    } while (0)
+#else
+#define KMC_SECTION(k) do { } while (0)
+#endif
+
 #ifndef KMC_PAIR_UNROLL
 #define KMC_PAIR_UNROLL 4
 #endif
@@ -585,6 +602,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     int64_t rbase = INT64_MIN / 2;
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
 
+#ifdef KMC_SECTION_CLOCKS
+    uint32_t sec_cycles[kSections] = {};
+    uint32_t sec_last = static_cast<uint32_t>(clock());
+#endif
     while (hop < hop_end) {
         if ((hop & 1023) == 0 && (B.cancel || (B.time_budget_ns > 0 && hop != hops_done0))) {
             // the host's cancel word, then the launch's wall-clock budget
@@ -604,6 +625,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             until_anchor = reanchor;
         }
         --until_anchor;
+        KMC_SECTION(0);
         // ---- pair phase ----
         const int z = N - h;
         const int T1 = z + P, T2 = z;
@@ -673,6 +695,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             }
         }
         npairs += static_cast<unsigned long long>(A);
+        KMC_SECTION(1);
         // ---- uniforms for this hop ----
         F2 u_ev;
         float e1;
@@ -695,6 +718,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             u_ev = grp.bcast2(rnd_u, ri);
         }
         if (sm.rates) grp.sync();   // stored rates visible to the whole group
+        KMC_SECTION(2);
         // ---- double-float scan of the per-thread sums ----
         F2 excl, tot;
         const F2 incl = grp.scan_df(lsum, excl, tot);
@@ -704,6 +728,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (L < 0) L = (A - 1) / M;   // u*total rounded above the total: the last non-empty run
         const F2 baseL = grp.bcast2(excl, L);
         float rem = df_add(target, F2{-baseL.hi, -baseL.lo}).hi;
+        KMC_SECTION(3);
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
@@ -766,11 +791,13 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 #ifdef KMC_DEBUG_CHECKS
         if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
 #endif
+        KMC_SECTION(4);
         // ---- clock ----
         const float dt = e1 * __frcp_rn(tot.hi);
         const double t_before = t;
         t += static_cast<double>(dt);
         grp.sync();   // every thread is done reading the lists and rates
+        KMC_SECTION(5);
         // ---- apply the hop and rebuild the lists in one pass ----
         const bool fa = from < N, tb = to < N;
         const int h_new = h + (tb ? 1 : 0) - (fa ? 1 : 0);
@@ -814,6 +841,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 }
             }
         }
+        KMC_SECTION(6);
         grp.sync();   // lists complete; the bitmask is read no more this hop
         if (g == 0) {
             if (fa) sm.occw[from >> 5] &= ~(1u << (from & 31));
@@ -828,6 +856,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 if (tb) occ_since[to] = tx;
             }
         }
+        KMC_SECTION(7);
         h = h_new;
         ++hop;
 #ifdef KMC_DEBUG_CHECKS
@@ -836,6 +865,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     }
     grp.sync();
 
+#ifdef KMC_SECTION_CLOCKS
+    if (g == 0) {
+        for (int k = 0; k < kSections; ++k) atomicAdd(&g_section_clocks[k], static_cast<unsigned long long>(sec_cycles[k]));
+        atomicAdd(&g_section_clocks[kSections], static_cast<unsigned long long>(hop - hops_done0));
+    }
+#endif
     // ---- write back ----
     if (record) {
         const double td = t;
@@ -1067,6 +1102,27 @@ int run_batch(const kmc_batch &b, cudaStream_t st)
         return dispatch<PositionPairs>(b, st);
     }
     return fail(KMC_ERR_INVALID, "engine: bad pair_mode %d", b.pair_mode);
+}
+
+int section_clocks(uint64_t *out, int reset)
+{
+#ifdef KMC_SECTION_CLOCKS
+    if (!out) return fail(KMC_ERR_INVALID, "section_clocks: out is NULL");
+    unsigned long long v[kSections + 1];
+    cudaError_t e = cudaMemcpyFromSymbol(v, g_section_clocks, sizeof(v));
+    if (e != cudaSuccess) return fail_cuda(e, "section_clocks read");
+    for (int k = 0; k <= kSections; ++k) out[k] = v[k];
+    if (reset) {
+        const unsigned long long z[kSections + 1] = {};
+        e = cudaMemcpyToSymbol(g_section_clocks, z, sizeof(z));
+        if (e != cudaSuccess) return fail_cuda(e, "section_clocks reset");
+    }
+    return KMC_OK;
+#else
+    (void)out;
+    (void)reset;
+    return fail(KMC_ERR_INVALID, "section_clocks: this library was built without -DKMC_SECTION_CLOCKS");
+#endif
 }
 
 }  // namespace kmc

@@ -19,6 +19,8 @@ int fail_cuda(cudaError_t e, const char *what);
 int ok();
 
 int run_batch(const kmc_batch &b, cudaStream_t st);
+// Per-phase cycle counters of a -DKMC_SECTION_CLOCKS build (9 values).
+int section_clocks(uint64_t *out, int reset);
 int engine_smem_words(int max_sites);
 int build_table(int N, int P, double nu, double I0, double R, const double *d, const double *tc,
                 float *tab, cudaStream_t st);

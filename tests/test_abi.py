@@ -55,6 +55,10 @@ def test_error_channel_without_gpu(engine_lib):
     assert code == rc and "bad sizes" in msg
     assert L.kmc_run_batch(None, None) == _native.KMC_ERR_INVALID
     assert L.kmc_version() >= 100
+    # the release library counts no section clocks (only a -DKMC_SECTION_CLOCKS build does)
+    out = (C.c_uint64 * 9)()
+    assert L.kmc_section_clocks(out, 0) == _native.KMC_ERR_INVALID
+    assert "KMC_SECTION_CLOCKS" in _native.last_error()[1]
 
 
 def _struct_fields(name):
