@@ -397,6 +397,7 @@ def main():
                             "unit": "Gexp/s", "frac": achieved / peak.value, "traffic": traffic,
                             "peak_source": "ex2.approx throughput measured live (kmc_measure_ex2_rate)",
                             "work": "allowed pairs A(h) summed over all hops of a launch, one ex2 each"},
+               "roofline_hbm": hbm_roofline(traffic, ms_per_step),
                "accuracy_vs_fp64": acc,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": launches_per_step * args.steps,
@@ -405,6 +406,26 @@ def main():
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def hbm_roofline(traffic, launch_ms):
+    """The same launch against the HBM roofline: its DRAM bytes (ncu) per
+    launch time, against the measured copy bandwidth (MEASURED_PEAKS.json, or
+    a 6.8 TB/s fallback).  The engine keeps tables and chain state on chip,
+    so this fraction is tiny: HBM is not what bounds the hop loop."""
+    if traffic is None:
+        return None
+    peak, src = 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            peak = float(json.load(open(path))["hbm_gbs"])
+            src = "of measured (MEASURED_PEAKS.json hbm_gbs)"
+        except (ValueError, KeyError):
+            pass
+    achieved = traffic / (launch_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_source": src}
 
 
 def run_e2e(net, V, hops, seed, lanes):
