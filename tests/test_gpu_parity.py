@@ -144,6 +144,33 @@ def test_f32_engine_same_alone_and_in_the_mix(engine_lib):
     np.testing.assert_array_equal(mix["occupation"][2], alone["occupation"][0])
 
 
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_f32_engine_register_variants_identical(engine_lib, lanes):
+    """A small launch runs the register-rich warp-slice variant (every block
+    resident at 2 per SM), a launch of many chains the 85-register one; the
+    same chain gives the same bits in both."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = workloads.plain_network(0)
+    spec = TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant)
+    rng = np.random.default_rng(8)
+
+    def run(n_chains, V):
+        b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, n.kT), [n.E_constant(v) for v in V],
+                  list(V), np.tile(n.occupation.astype(np.uint8), (n_chains, 1)), np.full(n_chains, 3000),
+                  seed=21, lanes=lanes, warps_per_block=8, record=2)
+        return b.run().results()
+    big = 16 * 152 * 32 // lanes + 64          # more warps than the SMs hold at 16 each
+    V = rng.uniform(-1, 1, (big, n.P))
+    small = run(48, V[:48])
+    large = run(big, V)
+    assert (small["status"] == 0).all() and (large["status"] == 0).all()
+    np.testing.assert_array_equal(small["time"], large["time"][:48])
+    for k in ("electrode_occupation", "occupation", "traffic", "occ_time"):
+        for x, y in zip(small[k], large[k][:48]):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_f32_engine_split_launches_identical(engine_lib):
     from kmc_dn_gb300 import workloads
     from kmc_dn_gb300.engine import Batch, TableSpec
