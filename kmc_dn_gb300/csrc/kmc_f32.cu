@@ -69,8 +69,8 @@ constexpr int kMaxElectrodes = 64;
 // with the SM clock; the group's thread 0 adds its per-phase cycle counts and
 // hop count to kSectionSlots device counters at the end of each launch
 // (kmc_section_clocks reads them).  Release builds compile them away.
-constexpr int kSections = 8;   // top, pairs, uniforms, scan, search, clock, rebuild, update
 #ifdef KMC_SECTION_CLOCKS
+constexpr int kSections = 8;   // top, pairs, uniforms, scan, search, clock, rebuild, update
 __device__ unsigned long long g_section_clocks[kSections + 1];
 #define KMC_SECTION(k)                                                   \
     do {                                                                 \
