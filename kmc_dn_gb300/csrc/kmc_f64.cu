@@ -81,7 +81,6 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
     uint8_t *occ = reinterpret_cast<uint8_t *>(red + 32);     // [S]
     __shared__ int ev_min;
     __shared__ double sh_total, sh_hop_time;
-    __shared__ int sh_stop;
 
     double *invd = ws;                  // [N*N] 1/d_ij
     double *ird = ws + (size_t)N * N;   // [N*N] (I_0 R)/d_ij
@@ -100,7 +99,6 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
         se[i] = se_in[i];
         occ[i] = (i < N) ? occ_g[i] : 0;
     }
-    if (tid == 0) sh_stop = 0;
     __syncthreads();
 
     const int chunk = (SS + kThreads - 1) / kThreads;

@@ -38,7 +38,6 @@ namespace kmc {
 namespace {
 
 constexpr int kMfThreads = 128;
-constexpr int kMfWarps = kMfThreads / 32;
 constexpr int kMfSmemLimit = 226 * 1024;   // dynamic; leaves room for the static words
 
 __device__ __forceinline__ double warp_sum(double x)
