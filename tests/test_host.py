@@ -104,3 +104,26 @@ def test_autotune_size_classes_and_candidates():
     assert autotune._candidates(38) == [4, 8, 16, 32]
     assert autotune._candidates(212) == [4, 8, 16, 32, 64, 128, 256, 512]
     assert autotune._candidates(1008) == [64, 128, 256, 512]
+
+
+def test_instrumented_builds_are_exclusive():
+    from kmc_dn_gb300 import build
+    with pytest.raises(ValueError, match="one of"):
+        build.build(debug_checks=True, section_clocks=True)
+    assert build.DEBUG_LIB != build.CLOCKS_LIB != build.LIB
+
+
+def test_hbm_roofline_of_a_launch(tmp_path, monkeypatch):
+    """The headline line's HBM roofline: DRAM bytes per launch time against
+    the measured copy bandwidth, or the stated fallback without it."""
+    import bench
+    r = bench.hbm_roofline(2_000_000, 4.0)           # 2 MB in 4 ms = 0.5 GB/s
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and abs(r["achieved"] - 0.5) < 1e-12
+    assert r["frac"] == r["achieved"] / r["peak"]
+    assert bench.hbm_roofline(None, 4.0) is None
+    monkeypatch.setattr(bench, "HERE", str(tmp_path))   # no MEASURED_PEAKS.json there
+    r = bench.hbm_roofline(2_000_000, 4.0)
+    assert r["peak"] == 6800.0 and "fallback" in r["peak_source"]
+    (tmp_path / "MEASURED_PEAKS.json").write_text('{"hbm_gbs": 5000.0}')
+    r = bench.hbm_roofline(2_000_000, 4.0)
+    assert r["peak"] == 5000.0 and r["peak_source"].startswith("of measured")
