@@ -75,3 +75,30 @@ def test_go_restatement_statistics(oracle_mod):
     sig = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps) + 1e-12
     z = np.abs(a.mean(0) - b.mean(0)) / sig
     assert np.all(z < 4.5), z
+
+
+def test_golden_pin_detects_planted_mistakes(oracle_mod):
+    """The golden comparison is not vacuous: mistakes planted in the oracle's
+    inputs on the CPU (uniforms consumed event-then-clock instead of
+    clock-then-event, a 0.1 % temperature error, two acceptors' distance rows
+    exchanged) each change the replayed hop sequence."""
+    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+    N, P = int(g["N"]), int(g["P"])
+    hops = 20000
+    u = replay_uniforms(int(g["seed"]), 2 * hops)
+    want = g["hop_log"][:hops].astype(np.int32)
+
+    def replay(u_, kT=float(g["kT"]), d=g["distances"]):
+        r = oracle_mod.numba_replay(N, P, float(g["nu"]), kT, float(g["I_0"]), float(g["R"]), g["occupation"],
+                                    d, g["E_constant"], g["site_energies"], g["transitions_constant"], u_,
+                                    hops=hops, record=False)
+        return r["hop_log"]
+
+    np.testing.assert_array_equal(replay(u), want)                  # the unplanted oracle agrees
+    swapped = u.reshape(-1, 2)[:, ::-1].reshape(-1).copy()
+    assert not np.array_equal(replay(swapped), want)
+    assert not np.array_equal(replay(u, kT=float(g["kT"]) * 1.001), want)
+    d = np.array(g["distances"], np.float64).reshape(N + P, N + P).copy()
+    d[[0, 1]] = d[[1, 0]]
+    d[:, [0, 1]] = d[:, [1, 0]]
+    assert not np.array_equal(replay(u, d=d), want)
