@@ -53,16 +53,13 @@ def test_pure_python_restatement_agrees(oracle_mod):
     assert abs(r["time"] - t) <= 1e-12 * abs(t)
 
 
-def test_go_restatement_statistics(oracle_mod):
-    """The FP32 Go-path restatement agrees with the FP64 numba restatement in
-    distribution: electrode currents over independent seeds within 4 sigma."""
-    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+def _current_z(oracle_mod, g, go_kT, hops=20000, reps=8):
+    """z-scores of the electrode-current differences between the FP32 Go-path
+    restatement (at temperature go_kT) and the FP64 numba restatement."""
     N, P = int(g["N"]), int(g["P"])
-    hops = 20000
-    reps = 8
     cur_go, cur_nb = [], []
     for s in range(reps):
-        r = oracle_mod.go_simulate(N, P, float(g["nu"]), float(g["kT"]), float(g["I_0"]), float(g["R"]),
+        r = oracle_mod.go_simulate(N, P, float(g["nu"]), go_kT, float(g["I_0"]), float(g["R"]),
                                    g["occupation"], g["distances"], g["E_constant"], g["site_energies"],
                                    g["transitions_constant"], hops, seed=1000 + s)
         cur_go.append(r["electrode_occupation"] / r["time"])
@@ -73,8 +70,23 @@ def test_go_restatement_statistics(oracle_mod):
         cur_nb.append(q["electrode_occupation"] / q["time"])
     a, b = np.array(cur_go), np.array(cur_nb)
     sig = np.sqrt(a.var(0, ddof=1) / reps + b.var(0, ddof=1) / reps) + 1e-12
-    z = np.abs(a.mean(0) - b.mean(0)) / sig
+    return np.abs(a.mean(0) - b.mean(0)) / sig
+
+
+def test_go_restatement_statistics(oracle_mod):
+    """The FP32 Go-path restatement agrees with the FP64 numba restatement in
+    distribution: electrode currents over independent seeds within 4.5 sigma."""
+    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+    z = _current_z(oracle_mod, g, float(g["kT"]))
     assert np.all(z < 4.5), z
+
+
+def test_current_comparison_detects_a_planted_bias(oracle_mod):
+    """The same z statistic flags a planted mistake: the Go-path restatement
+    run at twice the temperature gives currents the comparison rejects."""
+    g = load_golden([p for p in REPLAYS if "plain" in p][0])
+    z = _current_z(oracle_mod, g, 2.0 * float(g["kT"]))
+    assert np.any(z > 4.5), z
 
 
 def test_golden_pin_detects_planted_mistakes(oracle_mod):
