@@ -127,3 +127,62 @@ def test_hbm_roofline_of_a_launch(tmp_path, monkeypatch):
     (tmp_path / "MEASURED_PEAKS.json").write_text('{"hbm_gbs": 5000.0}')
     r = bench.hbm_roofline(2_000_000, 4.0)
     assert r["peak"] == 5000.0 and r["peak_source"].startswith("of measured")
+
+
+def _admission_server(mem_budget, long_thread_budget):
+    """A Server with only its admission state (no device): _prepare records
+    the admitted request and books its memory, chains and threads."""
+    from collections import deque
+    from types import SimpleNamespace
+    from kmc_dn_gb300.serving import Server, _request_bytes
+    s = object.__new__(Server)
+    s.networks = [SimpleNamespace(N=30, P=8), SimpleNamespace(N=240, P=8)]
+    s.queue, s.active, s.admitted = deque(), [], []
+    s.lanes, s.short_lanes_factor, s.short_hops = None, 4, 20000
+    s.mem_budget, s.mem_used = mem_budget, 0
+    s.max_active_chains, s.active_chains = 16384, 0
+    s.long_thread_budget, s.active_long_threads = long_thread_budget, 0
+
+    def prepare(req, need):
+        s.admitted.append(req)
+        s.active.append(req)
+        s.mem_used += need
+        s.active_chains += req.voltages.shape[0]
+        if req.hops > s.short_hops:
+            s.active_long_threads += s._threads(req)
+    s._prepare = prepare
+    return s, _request_bytes
+
+
+def test_admission_least_work_first_within_the_memory_budget():
+    from kmc_dn_gb300.serving import Request
+    s, nbytes = _admission_server(mem_budget=10**12, long_thread_budget=10**9)
+    big = Request(1, np.zeros((512, 8)), 10**6, 1)
+    small = Request(0, np.zeros((32, 8)), 10**4, 2)
+    mid = Request(0, np.zeros((512, 8)), 10**5, 3)
+    s.queue.extend([big, small, mid])
+    s._admit()
+    assert s.admitted == [small, mid, big]          # least chains x hops x pairs first
+    # a budget that holds the first two only: the third waits
+    s, nbytes = _admission_server(mem_budget=nbytes(32, 30, 8) + nbytes(512, 30, 8), long_thread_budget=10**9)
+    s.queue.extend([big, small, mid])
+    s._admit()
+    assert s.admitted == [small, mid] and list(s.queue) == [big]
+
+
+def test_admission_caps_long_requests_but_not_short_ones():
+    """Long requests may hold only the long-thread budget; a short request
+    behind them is still admitted on arrival."""
+    from kmc_dn_gb300.engine import default_lanes
+    from kmc_dn_gb300.serving import Request
+    threads = 512 * default_lanes(248)               # one 512-chain N=240 long request
+    s, _ = _admission_server(mem_budget=10**12, long_thread_budget=int(1.5 * threads))
+    long_a = Request(1, np.zeros((512, 8)), 10**6, 1)
+    long_b = Request(1, np.zeros((512, 8)), 10**6, 2)
+    short = Request(1, np.zeros((512, 8)), 10**4, 3)
+    s.queue.extend([long_a, long_b])
+    s._admit()
+    assert s.admitted == [long_a] and list(s.queue) == [long_b]   # the second would exceed the budget
+    s.queue.append(short)
+    s._admit()
+    assert s.admitted == [long_a, short] and list(s.queue) == [long_b]
