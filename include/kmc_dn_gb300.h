@@ -92,10 +92,17 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
  *   - The workspace is a fixed array inside this library: networks of at
  *     most 128 sites (N + P); larger ones return KMC_ERR_INVALID with a
  *     message.  The array (384 KiB) stays resident on every device that
- *     loads the library until the process exits.
- *   - The first call on a device looks the array's device address up
- *     (cudaGetSymbolAddress) and caches it; make that first call before any
- *     stream capture on that device.
+ *     loads the library's device code until the process exits.
+ *   - Under CUDA's default lazy module loading the device code (and with it
+ *     the array) is loaded into a context at its first use there, which
+ *     for a caller of this entry alone is its first call on a device: that
+ *     first call does take device memory.  Make one warm-up call on each
+ *     device (or load with CUDA_MODULE_LOADING=EAGER) before your own pool
+ *     takes the device, and before any stream capture on it.  Later calls
+ *     allocate nothing.
+ *   - Every call looks the array's device address up in the current
+ *     context (cudaGetSymbolAddress), so the entry stays valid after a
+ *     cudaDeviceReset and in a non-primary context.
  *   - All calls share the one array: calls whose kernels overlap on the
  *     device (different streams, or host threads) race and corrupt each
  *     other's results.  Serialise them on one stream.

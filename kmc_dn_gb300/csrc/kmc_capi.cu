@@ -62,7 +62,17 @@ struct EngineState {
     cudaStream_t st = nullptr;
     bool own_stream = false;
     std::vector<void *> ptrs;
-    kmc_batch b;
+    kmc_batch b;                       // shared pools; lanes/work/max_sites per bin below
+    // One launch per size class: lanes per chain, its work list and the
+    // largest network of the class.  Classes after the first run on their own
+    // streams, forked from and joined back to `st` with events.
+    struct Bin {
+        int32_t lanes = 0, n_work = 0, max_sites = 0;
+        int32_t *work = nullptr;
+    };
+    std::vector<Bin> bins;
+    std::vector<cudaStream_t> bin_streams;
+    std::vector<cudaEvent_t> bin_events;   // [0] fork, [1 + k] join of bin k + 1
     int32_t n_chains = 0;
     int64_t nsite = 0, nel = 0, npair = 0, maxhops = 0;
     int record = 0;
@@ -74,8 +84,24 @@ struct EngineState {
             cudaStreamSynchronize(st);
             if (own_stream) cudaStreamDestroy(st);
         }
+        for (cudaStream_t s : bin_streams) cudaStreamDestroy(s);
+        for (cudaEvent_t e : bin_events) cudaEventDestroy(e);
     }
 };
+
+// Lanes per chain of every chain: the caller's choice for all, or by size.
+// Chains are binned by it and ordered inside a bin by size, then hop budget
+// (both descending), so that chains sharing a warp have similar per-hop work
+// and lifetimes -- the order of the Python Batch's work lists.
+static std::vector<int> chain_lanes(const HostRun &h)
+{
+    std::vector<int> g(h.n_chains);
+    for (int c = 0; c < h.n_chains; ++c) {
+        const int geo = h.chain_geom[c];
+        g[c] = h.lanes_per_chain > 0 ? h.lanes_per_chain : auto_lanes(h.geom_N[geo] + h.geom_P[geo]);
+    }
+    return g;
+}
 
 int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
 {
@@ -135,21 +161,35 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
         tabid[c] = g;
         streams[c] = h.streams ? h.streams[c] : static_cast<uint64_t>(c);
     }
-    const int G = h.lanes_per_chain > 0 ? h.lanes_per_chain : auto_lanes(Smax);
-    if (G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128 && G != 256 && G != 512)
-        return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d", G);
-    const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
-    std::vector<int32_t> order(n_chains);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int sa = geom_N[chain_geom[a]] + geom_P[chain_geom[a]];
-        const int sb = geom_N[chain_geom[b]] + geom_P[chain_geom[b]];
-        if (sa != sb) return sa > sb;
-        return hops[a] > hops[b];
-    });
-    const int n_work = (n_chains + CPW - 1) / CPW;
-    std::vector<int32_t> work((size_t)n_work * CPW, -1);
-    for (int c = 0; c < n_chains; ++c) work[c] = order[c];
+    const std::vector<int> lanes_of = chain_lanes(h);
+    std::vector<int> lane_set(lanes_of);
+    std::sort(lane_set.begin(), lane_set.end());
+    lane_set.erase(std::unique(lane_set.begin(), lane_set.end()), lane_set.end());
+    for (int G : lane_set)
+        if (G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128 && G != 256 && G != 512)
+            return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d", G);
+    const auto site_count = [&](int c) { return geom_N[chain_geom[c]] + geom_P[chain_geom[c]]; };
+    // per bin (ascending lanes): its chains by size then hops, descending
+    std::vector<std::vector<int32_t>> bin_work(lane_set.size());
+    std::vector<int> bin_smax(lane_set.size(), 0);
+    for (size_t k = 0; k < lane_set.size(); ++k) {
+        const int G = lane_set[k];
+        std::vector<int32_t> order;
+        for (int c = 0; c < n_chains; ++c)
+            if (lanes_of[c] == G) order.push_back(c);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            const int sa = site_count(a), sb = site_count(b);
+            if (sa != sb) return sa > sb;
+            return hops[a] > hops[b];
+        });
+        const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
+        const size_t n_work = (order.size() + CPW - 1) / CPW;
+        bin_work[k].assign(n_work * CPW, -1);
+        for (size_t i = 0; i < order.size(); ++i) {
+            bin_work[k][i] = order[i];
+            bin_smax[k] = std::max(bin_smax[k], site_count(order[i]));
+        }
+    }
     std::vector<int64_t> poff(n_chains);
     int64_t npair = 0;
     for (int c = 0; c < n_chains; ++c) {
@@ -180,7 +220,7 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
     };
     double *d_dist = nullptr, *d_tc = nullptr;
     float *d_tab = nullptr, *d_ec = nullptr, *d_vel = nullptr, *d_kT = nullptr;
-    int32_t *d_tabN = nullptr, *d_tabP = nullptr, *d_ctab = nullptr, *d_status = nullptr, *d_work = nullptr;
+    int32_t *d_tabN = nullptr, *d_tabP = nullptr, *d_ctab = nullptr, *d_status = nullptr;
     int64_t *d_taboff = nullptr, *d_soff = nullptr, *d_eoff = nullptr, *d_eo = nullptr;
     int64_t *d_hd = nullptr, *d_ht = nullptr;
     uint8_t *d_occ = nullptr;
@@ -208,9 +248,30 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
         (e = dalloc((void **)&d_hd, sizeof(int64_t) * n_chains)) != cudaSuccess ||
         (e = dalloc((void **)&d_ht, sizeof(int64_t) * n_chains)) != cudaSuccess ||
         (e = dalloc((void **)&d_stream, sizeof(uint64_t) * n_chains)) != cudaSuccess ||
-        (e = dalloc((void **)&d_status, sizeof(int32_t) * n_chains)) != cudaSuccess ||
-        (e = dalloc((void **)&d_work, sizeof(int32_t) * work.size())) != cudaSuccess)
+        (e = dalloc((void **)&d_status, sizeof(int32_t) * n_chains)) != cudaSuccess)
         return fail_cuda(e, "engine: device allocation");
+    E->bins.resize(lane_set.size());
+    for (size_t k = 0; k < lane_set.size(); ++k) {
+        EngineState::Bin &bn = E->bins[k];
+        bn.lanes = lane_set[k];
+        bn.max_sites = bin_smax[k];
+        bn.n_work = static_cast<int32_t>(bin_work[k].size() / (bn.lanes >= 32 ? 1 : 32 / bn.lanes));
+        if ((e = dalloc((void **)&bn.work, sizeof(int32_t) * bin_work[k].size())) != cudaSuccess ||
+            (e = h2d(bn.work, bin_work[k].data(), sizeof(int32_t) * bin_work[k].size())) != cudaSuccess)
+            return fail_cuda(e, "engine: work lists");
+    }
+    for (size_t k = 1; k < lane_set.size(); ++k) {
+        cudaStream_t bs = nullptr;
+        if ((e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail_cuda(e, "engine: bin stream");
+        E->bin_streams.push_back(bs);
+    }
+    for (size_t k = 0; k < lane_set.size(); ++k) {
+        cudaEvent_t ev = nullptr;
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+            return fail_cuda(e, "engine: bin event");
+        E->bin_events.push_back(ev);
+    }
     if (record) {
         if ((e = dalloc((void **)&d_poff, sizeof(int64_t) * n_chains)) != cudaSuccess ||
             (e = dalloc((void **)&d_ot, sizeof(double) * std::max<int64_t>(nsite, 1))) != cudaSuccess ||
@@ -235,8 +296,7 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
         (e = h2d(d_eoff, el_off.data(), sizeof(int64_t) * n_chains)) != cudaSuccess ||
         (e = h2d(d_occ, occupation, (size_t)nsite)) != cudaSuccess ||
         (e = h2d(d_ht, hops, sizeof(int64_t) * n_chains)) != cudaSuccess ||
-        (e = h2d(d_stream, streams.data(), sizeof(uint64_t) * n_chains)) != cudaSuccess ||
-        (e = h2d(d_work, work.data(), sizeof(int32_t) * work.size())) != cudaSuccess)
+        (e = h2d(d_stream, streams.data(), sizeof(uint64_t) * n_chains)) != cudaSuccess)
         return fail_cuda(e, "engine: copy in");
     if ((e = cudaMemsetAsync(d_eo, 0, sizeof(int64_t) * std::max<int64_t>(nel, 1), st)) != cudaSuccess ||
         (e = cudaMemsetAsync(d_time, 0, sizeof(double) * n_chains, st)) != cudaSuccess ||
@@ -259,7 +319,6 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
     b.tab_off = d_taboff;
     b.tab_LB = d_tab;
     b.n_chains = n_chains;
-    b.lanes_per_chain = G;
     b.chain_tab = d_ctab;
     b.chain_kT = d_kT;
     b.chain_site_off = d_soff;
@@ -273,8 +332,6 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
     b.hops_total = d_ht;
     b.stream = d_stream;
     b.status = d_status;
-    b.work = d_work;
-    b.n_work = n_work;
     b.record = record;
     b.chain_pair_off = d_poff;
     b.occ_time = d_ot;
@@ -302,7 +359,30 @@ int engine_run(EngineState &E, int64_t max_hops)
     int64_t seg = max_hops > 0 ? max_hops : E.maxhops;
     seg = std::max<int64_t>(reanchor, ((seg + reanchor - 1) / reanchor) * reanchor);
     E.b.max_hops_per_launch = seg;
-    return run_batch(E.b, E.st);
+    const size_t nb = E.bins.size();
+    cudaError_t e;
+    if (nb > 1) {   // fork: the other bins' streams start after the work queued on st
+        if ((e = cudaEventRecord(E.bin_events[0], E.st)) != cudaSuccess) return fail_cuda(e, "engine: fork");
+        for (size_t k = 1; k < nb; ++k)
+            if ((e = cudaStreamWaitEvent(E.bin_streams[k - 1], E.bin_events[0], 0)) != cudaSuccess)
+                return fail_cuda(e, "engine: fork");
+    }
+    for (size_t k = 0; k < nb; ++k) {
+        const EngineState::Bin &bn = E.bins[k];
+        kmc_batch b = E.b;
+        b.lanes_per_chain = bn.lanes;
+        b.max_sites = bn.max_sites;
+        b.work = bn.work;
+        b.n_work = bn.n_work;
+        const int rc = run_batch(b, k == 0 ? E.st : E.bin_streams[k - 1]);
+        if (rc != KMC_OK) return rc;
+    }
+    for (size_t k = 1; k < nb; ++k) {   // join back onto st
+        if ((e = cudaEventRecord(E.bin_events[k], E.bin_streams[k - 1])) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(E.st, E.bin_events[k], 0)) != cudaSuccess)
+            return fail_cuda(e, "engine: join");
+    }
+    return KMC_OK;
 }
 
 // Copy results to the host (synchronises the engine's stream).  traffic_out

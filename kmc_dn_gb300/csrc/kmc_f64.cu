@@ -12,7 +12,11 @@
 //              dE = E_j - E_i - (I_0 R)/d_ij for acceptor pairs (:69-87)
 //   cumulative row-major running sum; each thread owns a contiguous chunk
 //              and continues the running sum from the FP64 prefix of the
-//              chunks before it (:91-97)
+//              chunks before it (:91-97).  That prefix is a tree sum of the
+//              chunk totals, not the reference's strictly left-to-right sum,
+//              so cum_k and the total may differ in the last bit: the hop
+//              sequence is the reference's except where u2 lies within a
+//              few ulp of a boundary cum_k/total
 //   clock      dt = -log(1 - u1) * (1/total) (:100)
 //   event      first k with cum_k/total >= u2 (:103-110)
 //   record     traffic[from,to] += 1, post-hop occupancy credit (:126-130)
@@ -20,7 +24,6 @@
 // This is the baseline kernel the batched FP32 engine is measured against,
 // and the kernel of the bit-exact replay check.
 #include <cstdint>
-#include <mutex>
 #include <cuda_runtime.h>
 
 #include "kmc_common.cuh"
@@ -246,30 +249,17 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
 constexpr int kStaticWorkspaceSites = 128;
 static __device__ __align__(256) double g_f64_static_workspace[3 * kStaticWorkspaceSites * kStaticWorkspaceSites];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_ws_mutex;
-double *g_ws_ptr[kMaxDevices] = {};
-}  // namespace
-
-// Device address of the static workspace on the current device.  The array's
-// name is only a host-side stand-in in host code, so the address is looked up
-// once per device (with that device current) and cached.
+// Device address of the static workspace in the current context.  The
+// array's name is only a host-side stand-in in host code, so its address is
+// looked up on every call (cheap once the module is loaded).  It is not
+// cached: after a cudaDeviceReset, or in another context on the same device,
+// the module is loaded again at a different address.
 static int static_workspace(double **out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail_cuda(e, "simulate_f64_static: cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices)
-        return fail(KMC_ERR_INVALID, "simulate_f64_static: device %d beyond the %d this library tracks", dev, kMaxDevices);
-    std::lock_guard<std::mutex> lock(g_ws_mutex);
-    if (!g_ws_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_f64_static_workspace);
-        if (e != cudaSuccess) return fail_cuda(e, "simulate_f64_static: cudaGetSymbolAddress");
-        g_ws_ptr[dev] = static_cast<double *>(p);
-    }
-    *out = g_ws_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_f64_static_workspace);
+    if (e != cudaSuccess) return fail_cuda(e, "simulate_f64_static: cudaGetSymbolAddress");
+    *out = static_cast<double *>(p);
     return KMC_OK;
 }
 

@@ -37,10 +37,16 @@ double single_chain(int64_t NSites, int64_t NElectrodes, double prune, double nu
         (record && (traffic.len < S * S || average_occupation.len < N)))
         return fail(KMC_ERR_INVALID, "Go-compatible call: slice lengths do not match N=%d P=%d", N, P);
     std::vector<double> tc(transitions_constant.data, transitions_constant.data + S * S);
-    if (prune > 0) {   // simulation.go:199-215: keep tc > cut * max(tc)
-        const double mx = *std::max_element(tc.begin(), tc.end());
+    if (prune > 0) {
+        // simulation.go:199-215 keeps the pairs with tc > cut * max(tc), all
+        // three in float32 (the wrapper converts the tables and the cut to
+        // float32 first, simulationWrapper.go:37-56, :98-110); the product is
+        // rounded to float32 before the compare.
+        float mx = 0.0f;
+        for (double x : tc) mx = std::max(mx, static_cast<float>(x));
+        const float cut = static_cast<float>(static_cast<float>(prune) * mx);
         for (double &x : tc)
-            if (!(x > prune * mx)) x = 0.0;
+            if (!(static_cast<float>(x) > cut)) x = 0.0;
     }
     const int32_t gN = N, gP = P;
     const int64_t off = 0;

@@ -607,12 +607,16 @@ def simulate_cuda(N_acceptors, N_electrodes, nu, kT, I_0, R, time, occupation, d
 
 
 def prune(transitions_constant, threshold):
-    """Zero the pairs a pruned Go run leaves out of its transition list:
-    ``tc <= threshold * max(tc)`` (simulation.go:199-215).  A zero constant
-    gives a zero rate, so the pair can never be selected."""
+    """Zero the pairs a pruned Go run leaves out of its transition list: it
+    keeps ``tc > threshold * max(tc)`` (simulation.go:199-215), all in
+    float32 as the Go code holds them (the product rounded to float32 before
+    the compare).  A zero constant gives a zero rate, so a pruned pair can
+    never be selected."""
     tc = np.array(transitions_constant, dtype=np.float64, copy=True)
     if threshold and threshold > 0:
-        tc[tc <= threshold * tc.max()] = 0.0
+        t32 = tc.astype(np.float32)
+        cut = np.float32(np.float32(threshold) * np.float32(t32.max()))
+        tc[~(t32 > cut)] = 0.0
     return tc
 
 

@@ -108,3 +108,96 @@ def test_parallel_simulations_through_reference_argtypes(engine_lib):
     eo = arrays["electrode_occupation"].reshape(nc, P)
     # hole number conservation per chain: electrodes absorb what acceptors lose
     assert np.all(np.abs(eo.sum(1)) <= N)
+
+
+PRUNE_CUT = 1e-2     # drops 58 % of this network's pairs, the far ones
+
+
+def _pruned_mask(n, cut):
+    from kmc_dn_gb300.engine import prune
+    return prune(n.transitions_constant, cut) == 0.0
+
+
+def test_wrapper_simulate_pruned_through_reference_argtypes(engine_lib, oracle_mod):
+    """wrapperSimulatePruned (simulation.go:199-215, simulationWrapper.go:
+    98-110) called with pythonBind's argtypes for it (the cut as the third
+    argument): no traffic on any pair the cut removes, net traffic
+    antisymmetric, and the electrode currents of repeated calls within 3
+    sigma of the oracle's restatement of the Go loop run on the same pruned
+    constants (both start empty, both run the same hop budget)."""
+    n = _net()
+    N, P, S = n.N, n.P, n.S
+    lib = lib_as_go()
+    f = lib.wrapperSimulatePruned
+    f.argtypes = [C.c_longlong, C.c_longlong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                  C.c_double, GoSlice, GoSlice, GoSlice, GoSlice, GoSlice, GoSlice, C.c_int, C.c_bool,
+                  GoSlice, GoSlice]
+    f.restype = C.c_double
+    pruned = _pruned_mask(n, PRUNE_CUT)
+    hops, calls, reps = 20000, 24, 48
+    keep = []
+    sl = lambda a: (lambda s_a: (keep.append(s_a[1]), s_a[0])[1])(slice_of(a))  # noqa: E731
+    cur = []
+    for _ in range(calls):
+        eo_arr, tr_arr, av_arr = np.zeros(P), np.zeros(S * S), np.zeros(N)
+        eo = GoSlice(eo_arr.ctypes.data_as(C.POINTER(C.c_double)), P, P)
+        tr = GoSlice(tr_arr.ctypes.data_as(C.POINTER(C.c_double)), S * S, S * S)
+        av = GoSlice(av_arr.ctypes.data_as(C.POINTER(C.c_double)), N, N)
+        t = f(N, P, PRUNE_CUT, n.nu, n.kT, n.I_0, n.R, 0.0, sl(n.occupation.astype(float)),
+              sl(n.distances.ravel()), sl(n.E_constant()), sl(n.transitions_constant.ravel()), eo,
+              sl(n.site_energies()), hops, True, tr, av)
+        assert t > 0, t
+        traffic = tr_arr.reshape(S, S)
+        assert np.all(traffic[pruned] == 0), "a pruned pair carried traffic"
+        np.testing.assert_allclose(traffic, -traffic.T)
+        np.testing.assert_allclose(eo_arr, traffic[:, N:].sum(axis=0))
+        cur.append(eo_arr / t)
+    cur = np.array(cur)
+    from kmc_dn_gb300.engine import prune
+    tcp = prune(n.transitions_constant, PRUNE_CUT)
+    ref = []
+    for s in range(reps):
+        o = oracle_mod.go_simulate(N, P, n.nu, n.kT, n.I_0, n.R, np.zeros(N, np.uint8), n.distances,
+                                   n.E_constant(), n.site_energies(), tcp, hops, seed=700 + s, record=True)
+        assert np.all(o["traffic"][pruned] == 0)
+        ref.append(o["electrode_occupation"] / o["time"])
+    ref = np.array(ref)
+    se = np.sqrt(cur.var(0, ddof=1) / calls + ref.var(0, ddof=1) / reps)
+    z = np.abs(cur.mean(0) - ref.mean(0)) / np.maximum(se, 1e-300)
+    assert np.all(z < 3.5), z
+
+
+def test_go_simulation_pruned_matches_oracle(engine_lib, oracle_mod):
+    """kmc_dn.go_simulation(goSpecificFunction="wrapperSimulatePruned",
+    prune_threshold=cut) on the FP32 engine: no traffic on pruned pairs, and
+    the currents of many such runs (the same code path, batched) within 3
+    sigma of the oracle's Go loop on the same pruned constants."""
+    from kmc_dn_gb300 import _native
+    from kmc_dn_gb300.engine import Batch, TableSpec, prune
+    from kmc_dn_gb300.kmc_dn import kmc_dn
+    n = _net()
+    N, P = n.N, n.P
+    pruned = _pruned_mask(n, PRUNE_CUT)
+    dn = kmc_dn(N, n.M, n.xdim, n.ydim, 0, electrodes=n.electrodes, acceptors=n.acceptors,
+                donors=n.donors, I_0=n.I_0 / n.kT, a=n.ab / n.R)
+    np.testing.assert_array_equal(dn.distances, n.distances)
+    dn.go_simulation(hops=20000, goSpecificFunction="wrapperSimulatePruned", prune_threshold=PRUNE_CUT,
+                     record=True, seed=5)
+    assert np.all(np.asarray(dn.traffic)[pruned] == 0)
+    hops, reps_gpu, reps_cpu = 20000, 256, 48
+    tcp = prune(n.transitions_constant, PRUNE_CUT)
+    spec = TableSpec(N, P, n.nu, n.I_0, n.R, n.distances, tcp)
+    b = Batch([spec], [0] * reps_gpu, [n.kT] * reps_gpu, [n.E_constant()] * reps_gpu,
+              [n.electrodes[:, 3]] * reps_gpu, [np.zeros(N, np.uint8)] * reps_gpu, [hops] * reps_gpu,
+              seed=31, record=_native.RECORD_GO)
+    r = b.run().results()
+    assert np.all(r["status"] == 0)
+    assert all(np.all(t[pruned] == 0) for t in r["traffic"])
+    cur = np.array([e / t for e, t in zip(r["electrode_occupation"], r["time"])])
+    ref = np.array([(lambda o: o["electrode_occupation"] / o["time"])(
+        oracle_mod.go_simulate(N, P, n.nu, n.kT, n.I_0, n.R, np.zeros(N, np.uint8), n.distances,
+                               n.E_constant(), n.site_energies(), tcp, hops, seed=900 + s))
+        for s in range(reps_cpu)])
+    se = np.sqrt(cur.var(0, ddof=1) / reps_gpu + ref.var(0, ddof=1) / reps_cpu)
+    z = np.abs(cur.mean(0) - ref.mean(0)) / np.maximum(se, 1e-300)
+    assert np.all(z < 3.5), z

@@ -355,3 +355,48 @@ def test_sizes_beyond_the_limits_are_rejected(engine_lib):
     with pytest.raises(ValueError, match="at most 64 electrodes"):
         Batch([spec], [0], [1.0], [net.E_constant()], [net.electrodes[:, 3]], [net.occupation.astype(np.uint8)],
               [10], lanes=128)
+
+
+def test_run_batch_host_bins_ragged_batches_like_python_batch(engine_lib):
+    """A ragged batch (networks of 10..200 acceptors, 4..12 electrodes, own
+    kT and hop budgets) through kmc_run_batch_host: the host path bins the
+    chains by size class (its own lanes per class, one launch per class, as
+    the reference's parallelSimulations takes ragged batches, goSimulation/
+    simulationWrapper.go:285-309) and gives the Python Batch's results bit
+    for bit."""
+    import ctypes as C
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300._native import lib, check
+    from kmc_dn_gb300.engine import Batch, TableSpec, default_lanes
+    nets = workloads.uneven_batch(40, seed=11, hops_range=(2000, 6000))
+    nc = len(nets)
+    assert len({default_lanes(net.S) for net, _ in nets}) >= 3        # at least three size classes
+    hops = np.array([h for _, h in nets], np.int64)
+    gN = np.array([net.N for net, _ in nets], np.int32)
+    gP = np.array([net.P for net, _ in nets], np.int32)
+    S = gN + gP
+    goff = np.concatenate([[0], np.cumsum(S.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+    dist = np.concatenate([net.distances.ravel() for net, _ in nets])
+    tc = np.concatenate([net.transitions_constant.ravel() for net, _ in nets])
+    ec = np.concatenate([net.E_constant() for net, _ in nets])
+    se = np.concatenate([net.site_energies() for net, _ in nets])
+    occ = np.concatenate([net.occupation.astype(np.uint8) for net, _ in nets])
+    kT = np.array([net.kT for net, _ in nets])
+    t_out = np.zeros(nc)
+    eo = np.zeros(int(gP.sum()), np.int64)
+    st = np.zeros(nc, np.int32)
+    seed = 4242
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(lib().kmc_run_batch_host(nc, p(gN), p(gP), p(np.array([n.nu for n, _ in nets])),
+                                   p(np.array([n.I_0 for n, _ in nets])), p(np.array([n.R for n, _ in nets])),
+                                   p(goff), p(dist), p(tc), nc, p(np.arange(nc, dtype=np.int32)), p(kT), p(ec),
+                                   p(se), p(occ), p(hops), seed, 0, p(t_out), p(eo), p(st)))
+    specs = [TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant) for n, _ in nets]
+    b = Batch(specs, np.arange(nc), kT, [n.E_constant() for n, _ in nets], [n.electrodes[:, 3] for n, _ in nets],
+              [n.occupation.astype(np.uint8) for n, _ in nets], hops, seed=seed)
+    assert len(b._bins) >= 3
+    r = b.run().results()
+    np.testing.assert_array_equal(st, 0)
+    np.testing.assert_array_equal(t_out, r["time"])
+    np.testing.assert_array_equal(eo, np.concatenate(r["electrode_occupation"]))
+    np.testing.assert_array_equal(occ.astype(bool), np.concatenate(r["occupation"]))

@@ -186,3 +186,15 @@ def test_admission_caps_long_requests_but_not_short_ones():
     s.queue.append(short)
     s._admit()
     assert s.admitted == [long_a, short] and list(s.queue) == [long_b]
+
+
+def test_prune_cut_is_taken_in_float32_as_go_does():
+    """simulation.go:199-215 keeps tc > cut * max(tc) with tc, the cut and
+    their product in float32: an entry a hair above the cut in FP64 that
+    rounds onto it in float32 is pruned, as in Go."""
+    from kmc_dn_gb300.engine import prune
+    tc = np.array([[0.0, 1.0, 0.1 + 1e-12], [1.0, 0.0, 0.25], [0.1 + 1e-12, 0.25, 0.0]])
+    p = prune(tc, 0.1)
+    assert p[0, 2] == 0.0 and p[2, 0] == 0.0          # float32(0.1 + 1e-12) == float32(0.1): not above
+    assert p[0, 1] == 1.0 and p[1, 2] == 0.25         # clearly above: kept with its FP64 value
+    np.testing.assert_array_equal(prune(tc, 0.0), tc)  # no cut: unchanged

@@ -126,3 +126,43 @@ def test_gpu_p1_sampling_matches_host(engine_lib):
     torch.cuda.synchronize()
     host = np.stack([interpolate_p1(f, bf, pts) for f in bf.fields])
     np.testing.assert_allclose(out.cpu().numpy().reshape(host.shape), host, rtol=1e-13, atol=1e-13)
+
+
+def _superpose_cases():
+    """The networks whose device superposition feeds the timed workloads: the
+    homogeneous ensemble's network with its first voltage vectors, and the
+    four serving geometries with populations of U[-1,1] vectors."""
+    from kmc_dn_gb300 import workloads
+    net, V = workloads.homogeneous_ensemble(64, 0)
+    cases = [("homogeneous", net, V)]
+    rng = np.random.default_rng(17)
+    for g in workloads.serving_geometries(seed=0):
+        cases.append((f"serving_N{g.N}", g, rng.uniform(-1, 1, (48, g.P))))
+    return cases
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(5), ids=["homogeneous", "serving_N30", "serving_N60",
+                                                "serving_N120", "serving_N240"])
+def test_device_superposition_matches_host_E_constant(engine_lib, case):
+    """kmc_site_energies (the device superposition that builds every timed
+    chain's constant site energies and every serving request's) equals the
+    host E_constant = V @ basis + mu * basis_mu + comp
+    (calc_E_constant_V_comp, kmc_dopant_networks.py:865-899) rounded to FP32.
+
+    Tolerance: the device sums the same FP64 terms in another order and
+    rounds once to FP32, so each value may land one FP32 ulp away from the
+    rounded host value: |dE| <= 2^-23 |E| (plus 1e-12 absolute for the FP64
+    summation order near E = 0).  Electrode energies are the voltages
+    rounded to FP32, exactly."""
+    from kmc_dn_gb300.engine import superpose
+    name, net, V = _superpose_cases()[case]
+    ec, ve = superpose(net.basis, net.comp, V, net.mu, dev="cuda")
+    ec = ec.cpu().numpy().reshape(V.shape[0], net.N).astype(np.float64)
+    ve = ve.cpu().numpy().reshape(V.shape[0], net.P)
+    host = np.stack([net.E_constant(v) for v in V])
+    err = np.abs(ec - host.astype(np.float32).astype(np.float64))
+    tol = 2.0 ** -23 * np.abs(host) + 1e-12
+    assert np.all(err <= tol), (name, float((err / np.maximum(tol, 1e-300)).max()))
+    assert np.max(np.abs(ec - host)) <= 2.0 ** -22 * np.max(np.abs(host)), name   # 2 ulp of max|E|
+    np.testing.assert_array_equal(ve, V.astype(np.float32))
