@@ -211,6 +211,18 @@ typedef struct kmc_batch {
      * state consistent, and a later launch resumes it as if uninterrupted.
      * 0: none */
     int64_t time_budget_ns;
+    /* optional per-hop log (replay tests, rate-level accuracy checks): the
+     * chain's absolute hop k (k < hops_total[c]) writes {from, to} to
+     * hop_log[2*(hop_log_off[c] + k)] and, when hop_rates is set, {total
+     * rate, rate of the chosen pair} as the engine computed them (FP32) to
+     * hop_rates[2*(hop_log_off[c] + k)].  NULL: no log */
+    int32_t *hop_log;
+    float *hop_rates;
+    const int64_t *hop_log_off;     /* [n_chains] offset in hops               */
+    /* debug builds only (-DKMC_DEBUG_CHECKS): per chain, hops whose event an
+     * FP64 scan and compare over the same FP32 per-thread sums would place
+     * on another pair than the engine's exact integer compare; NULL: off */
+    unsigned long long *select_mismatch;
 } kmc_batch;
 
 /*

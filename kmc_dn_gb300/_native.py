@@ -62,6 +62,7 @@ class KmcBatch(C.Structure):
         ("replay", _vp), ("replay_off", _vp), ("cancel", _vp),
         ("pair_mode", _i32), ("tab_pos", _vp), ("tab_pos_off", _vp), ("tab_coef", _vp),
         ("time_budget_ns", _i64),
+        ("hop_log", _vp), ("hop_rates", _vp), ("hop_log_off", _vp), ("select_mismatch", _vp),
     ]
 
 

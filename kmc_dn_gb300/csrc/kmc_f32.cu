@@ -174,6 +174,61 @@ __device__ __forceinline__ F2 u01_df(uint32_t a, uint32_t b)
     return F2{hi, lo};
 }
 
+// ---------------------------------------------------------------------------
+// Exact fixed-point selection.  The per-thread FP32 sums of a group are
+// converted to 64-bit integers on a common power-of-two scale set by the
+// largest of them (24 mantissa bits shifted left by kShift, so the group's
+// total stays below 2^62), scanned with integer adds, which are exact, and
+// compared with u * total computed exactly from a 64-bit fixed-point u.  The
+// comparison is therefore exact for the FP32 per-thread sums it is given:
+// finer than an FP64 compare, on the integer pipe.  Only a thread's own sum
+// below 2^-(23 + kShift) of the largest one is truncated (at most 2^-52 of
+// the total).
+// ---------------------------------------------------------------------------
+template <int G>
+struct FixShift {
+    static constexpr int kLog = G <= 4 ? 2 : G <= 8 ? 3 : G <= 16 ? 4 : G <= 32 ? 5 : G <= 64 ? 6 :
+                                G <= 128 ? 7 : G <= 256 ? 8 : 9;
+    static constexpr int kShift = 38 - kLog;   // 24 + kShift + log2(G) = 62
+};
+
+// v >= 0 (a sum of ex2 results) on the scale whose unit is
+// 2^(emax - 150 - shift), emax the biased exponent of the group's largest sum.
+__device__ __forceinline__ uint64_t to_fixed(float v, int emax, int shift)
+{
+    const uint32_t bits = __float_as_uint(v);
+    const int e = static_cast<int>(bits >> 23);
+    const uint64_t m = e ? static_cast<uint64_t>((bits & 0x7fffffu) | 0x800000u) : 0ull;
+    const int sh = e - emax + shift;
+    return sh >= 0 ? (m << sh) : (sh > -24 ? (m >> -sh) : 0ull);
+}
+
+// An integer on that scale back to FP32.
+__device__ __forceinline__ float from_fixed(uint64_t x, int emax, int shift)
+{
+    return ldexpf(__ull2float_rn(x), emax - 150 - shift);
+}
+
+// The first cumulative value that reaches u * total, u = uq * 2^-64: the
+// smallest integer >= uq * tot / 2^64.
+__device__ __forceinline__ uint64_t fixed_target(uint64_t uq, uint64_t tot)
+{
+    return __umul64hi(uq, tot) + ((uq * tot) != 0ull ? 1ull : 0ull);
+}
+
+// Event uniform in (0,1) as 64-bit fixed point: 47 random bits, (2A+1) 2^-48.
+__device__ __forceinline__ uint64_t u01_fixed(uint32_t a, uint32_t b)
+{
+    const uint64_t A = ((static_cast<uint64_t>(a) << 15) | (b >> 17)) & ((1ull << 47) - 1);
+    return ((A << 1) | 1ull) << 16;
+}
+
+// A replay uniform u in (0,1) as 64-bit fixed point (exact for u >= 2^-11).
+__device__ __forceinline__ uint64_t u01_fixed_from_double(double u)
+{
+    return __double2ull_rz(u * 0x1.0p64);
+}
+
 // k -> (row, col) within the pair enumeration.  Float-reciprocal quotient
 // with one correction step: with inv within 2^-22 (relative) of 1/T and
 // k < 2^22 the estimate is off by less than one, so the result is exact (the
@@ -202,15 +257,23 @@ __device__ __forceinline__ void decode_pair(int k, int h, int A1, int T1, int T2
 // ---------------------------------------------------------------------------
 
 // Table mode: records are {site, scaled energy}; (L, B) read from the table.
+// kStaged: the launch's one table sits in shared memory (the pointer then
+// derives from shared memory only, so its loads are shared-memory loads with
+// 32-bit addresses); otherwise each chain reads its table from global memory.
+template <bool kStaged>
 struct TablePairs {
     using Rec = int2;
     static constexpr bool kSiteInRec = true;    // rec.x is the site id
+    static constexpr bool kStagedTable = kStaged;
     __device__ __forceinline__ static int site(Rec r) { return r.x; }
     const float2 *tab;
     int S;
     __device__ __forceinline__ void init(const kmc_batch &B, int t_id, int S_, const float2 *shared_tab)
     {
-        tab = shared_tab ? shared_tab : reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
+        if (kStaged)
+            tab = shared_tab;
+        else
+            tab = reinterpret_cast<const float2 *>(B.tab_LB + B.tab_off[t_id]);
         S = S_;
     }
     __device__ __forceinline__ Rec rec(int site, float e) const { return make_int2(site, __float_as_int(e)); }
@@ -230,6 +293,7 @@ struct TablePairs {
 struct PositionPairs {
     using Rec = float4;
     static constexpr bool kSiteInRec = false;   // site ids kept beside the records
+    static constexpr bool kStagedTable = false;
     __device__ __forceinline__ static int site(Rec) { return -1; }
     const float4 *pos;
     float kL, L0, IR;
@@ -314,6 +378,35 @@ struct WarpGroup {
     {
         return F2{__shfl_sync(mask, v.hi, src, G), __shfl_sync(mask, v.lo, src, G)};
     }
+    __device__ __forceinline__ uint32_t max_u32(uint32_t v) const { return __reduce_max_sync(mask, v); }
+#ifdef KMC_DEBUG_CHECKS
+    // FP64 inclusive scan (debug builds: the cross-check of the selection)
+    __device__ double scan_f64(double v, double &excl, double &tot) const
+    {
+        double x = v;
+        for (int d = 1; d < G; d <<= 1) {
+            const double o = __shfl_up_sync(mask, x, d, G);
+            if (g >= d) x += o;
+        }
+        const double e = __shfl_up_sync(mask, x, 1, G);
+        excl = g == 0 ? 0.0 : e;
+        tot = __shfl_sync(mask, x, G - 1, G);
+        return x;
+    }
+#endif
+    // inclusive integer scan; sets the exclusive value and the total
+    __device__ __forceinline__ uint64_t scan_u64(uint64_t v, uint64_t &excl, uint64_t &tot) const
+    {
+        uint64_t x = v;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const uint64_t o = __shfl_up_sync(mask, x, d, G);
+            if (g >= d) x += o;
+        }
+        excl = x - v;
+        tot = __shfl_sync(mask, x, G - 1, G);
+        return x;
+    }
     // inclusive double-float scan of FP32 values; sets the exclusive value
     // and the total
     __device__ __forceinline__ F2 scan_df(float v, F2 &excl, F2 &tot) const
@@ -387,6 +480,76 @@ struct BlockGroup {
         const int r = si[1];
         __syncthreads();
         return r;
+    }
+#ifdef KMC_DEBUG_CHECKS
+    __device__ double scan_f64(double v, double &excl, double &tot) const
+    {
+        const int lane = g & 31, w = g >> 5;
+        double x = v;
+        for (int d = 1; d < 32; d <<= 1) {
+            const double o = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += o;
+        }
+        if (lane == 31) sd[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            double y = lane < kWarps ? sd[lane] : 0.0;
+            for (int d = 1; d < kWarps; d <<= 1) {
+                const double o = __shfl_up_sync(0xffffffffu, y, d);
+                if (lane >= d) y += o;
+            }
+            if (lane < kWarps) sd[lane] = y;
+        }
+        __syncthreads();
+        const double base = w > 0 ? sd[w - 1] : 0.0;
+        tot = sd[kWarps - 1];
+        __syncthreads();
+        x += base;
+        const double prev = __shfl_up_sync(0xffffffffu, x, 1);
+        excl = lane > 0 ? prev : base;
+        return x;
+    }
+#endif
+    __device__ uint32_t max_u32(uint32_t v) const
+    {
+        const uint32_t w = __reduce_max_sync(0xffffffffu, v);
+        uint32_t *s = reinterpret_cast<uint32_t *>(sd);   // kWarps slots
+        if ((g & 31) == 0) s[g >> 5] = w;
+        __syncthreads();
+        uint32_t m = s[0];
+#pragma unroll
+        for (int k = 1; k < kWarps; ++k) m = max(m, s[k]);
+        __syncthreads();
+        return m;
+    }
+    __device__ uint64_t scan_u64(uint64_t v, uint64_t &excl, uint64_t &tot) const
+    {
+        const int lane = g & 31, w = g >> 5;
+        uint64_t x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint64_t o = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += o;
+        }
+        uint64_t *s = reinterpret_cast<uint64_t *>(sd);   // kWarps slots
+        if (lane == 31) s[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            uint64_t y = lane < kWarps ? s[lane] : 0ull;
+#pragma unroll
+            for (int d = 1; d < kWarps; d <<= 1) {
+                const uint64_t o = __shfl_up_sync(0xffffffffu, y, d);
+                if (lane >= d) y += o;
+            }
+            if (lane < kWarps) s[lane] = y;
+        }
+        __syncthreads();
+        const uint64_t base = w > 0 ? s[w - 1] : 0ull;
+        tot = s[kWarps - 1];
+        __syncthreads();
+        x += base;
+        excl = x - v;
+        return x;
     }
     __device__ F2 scan_df(float v, F2 &excl, F2 &tot) const
     {
@@ -598,7 +761,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // Thread g holds the two uniforms of hop rbase + (g mod 32), already
     // mapped: the clock's Exp(1) variate and the event uniform.
     float rnd_e1 = 0.0f;
+#ifdef KMC_SELECT_DOUBLE_FLOAT
     F2 rnd_u{0.0f, 0.0f};
+#else
+    uint64_t rnd_u = 0;
+#endif
     int64_t rbase = INT64_MIN / 2;
     constexpr int RW = G < 32 ? G : 32;   // hops per refill
 
@@ -697,11 +864,19 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         npairs += static_cast<unsigned long long>(A);
         KMC_SECTION(1);
         // ---- uniforms for this hop ----
+#ifdef KMC_SELECT_DOUBLE_FLOAT
         F2 u_ev;
+#else
+        uint64_t u_ev;
+#endif
         float e1;
         if (replay) {
             e1 = -log1pf(-static_cast<float>(replay[2 * hop]));
+#ifdef KMC_SELECT_DOUBLE_FLOAT
             u_ev = df_from_double(replay[2 * hop + 1]);
+#else
+            u_ev = u01_fixed_from_double(replay[2 * hop + 1]);
+#endif
         } else {
             if (hop - rbase >= RW) {
                 rbase = hop;
@@ -711,24 +886,53 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                                                     static_cast<uint32_t>(stream >> 32)},
                                               k0, k1);
                 rnd_e1 = -__logf(u01_from32(w.x));
+#ifdef KMC_SELECT_DOUBLE_FLOAT
                 rnd_u = u01_df(w.y, w.z);
+#else
+                rnd_u = u01_fixed(w.y, w.z);
+#endif
             }
             const int ri = static_cast<int>(hop - rbase);
             e1 = grp.bcast(rnd_e1, ri);
+#ifdef KMC_SELECT_DOUBLE_FLOAT
             u_ev = grp.bcast2(rnd_u, ri);
+#else
+            u_ev = grp.bcast(rnd_u, ri);
+#endif
         }
         if (sm.rates) grp.sync();   // stored rates visible to the whole group
         KMC_SECTION(2);
+#ifdef KMC_SELECT_DOUBLE_FLOAT
         // ---- double-float scan of the per-thread sums ----
         F2 excl, tot;
         const F2 incl = grp.scan_df(lsum, excl, tot);
         if (!(tot.hi > 0.0f) || !(tot.hi <= 3.0e38f)) { status = KMC_ERR_NONFINITE; break; }
+        const float totf = tot.hi;
         const F2 target = df_mul(u_ev, tot);
         int L = grp.first(df_ge(incl, target));
         if (L < 0) L = (A - 1) / M;   // u*total rounded above the total: the last non-empty run
         const F2 baseL = grp.bcast2(excl, L);
         float rem = df_add(target, F2{-baseL.hi, -baseL.lo}).hi;
-        KMC_SECTION(3);
+#else
+        // ---- exact fixed-point scan of the per-thread sums ----
+        // scale: the largest per-thread sum (positive FP32 values order as
+        // their bit patterns; NaN and infinity sit above every finite value)
+        const uint32_t mx = grp.max_u32(__float_as_uint(lsum));
+        if (mx == 0u || mx >= 0x7f800000u) { status = KMC_ERR_NONFINITE; break; }
+        constexpr int kShift = FixShift<G>::kShift;
+        const int emax = static_cast<int>(mx >> 23);
+        uint64_t excl, tot;
+        const uint64_t incl = grp.scan_u64(to_fixed(lsum, emax, kShift), excl, tot);
+        const float totf = from_fixed(tot, emax, kShift);
+        if (!(totf <= 3.0e38f)) { status = KMC_ERR_NONFINITE; break; }
+        // the event is the first pair whose cumulative rate reaches u*total:
+        // thread L's run holds it (tot >= target, so some thread qualifies)
+        const uint64_t target = fixed_target(u_ev, tot);
+        int L = grp.first(incl >= target);
+        if (L < 0) L = (A - 1) / M;
+        // what remains of u*total beyond the runs before L, back in FP32
+        float rem = grp.bcast(from_fixed(target - excl, emax, kShift), L);
+#endif        KMC_SECTION(3);
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
@@ -778,6 +982,29 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         if (chosen < 0) chosen = last_pos;
         if (chosen < 0) { status = KMC_ERR_NONFINITE; break; }
+#if defined(KMC_DEBUG_CHECKS) && !defined(KMC_SELECT_DOUBLE_FLOAT)
+        if (B.select_mismatch && sm.rates) {
+            // the same selection with an FP64 scan and compare over the same
+            // FP32 per-thread sums: count the hops where it picks another pair
+            double dex, dtot;
+            const double dinc = grp.scan_f64(static_cast<double>(lsum), dex, dtot);
+            const double dtarget = __ull2double_rn(u_ev) * 0x1.0p-64 * dtot;
+            int L64 = grp.first(dinc >= dtarget);
+            if (L64 < 0) L64 = (A - 1) / M;
+            const float rem64 = grp.bcast(static_cast<float>(dtarget - dex), L64);
+            if (g == 0) {
+                const int len = min(M, A - L64 * M);
+                int c64 = -1, lp = -1;
+                for (int i = 0; i < len; ++i) {
+                    const float ri = sm.rates[i * G + L64];
+                    if (c64 < 0 && ri >= (rem64 > 0.0f ? rem64 : 1.0e-38f)) c64 = i;
+                    if (ri > (i > 0 ? sm.rates[(i - 1) * G + L64] : 0.0f)) lp = i;
+                }
+                if (c64 < 0) c64 = lp;
+                if (L64 * M + c64 != chosen) B.select_mismatch[c] += 1ull;
+            }
+        }
+#endif
         int row, col;
         KMC_DCHECK(chosen >= 0 && chosen < A && L >= 0 && L < G);
         decode_pair(chosen, h, A1, T1, T2, inv1, inv2, row, col);
@@ -791,9 +1018,18 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
 #ifdef KMC_DEBUG_CHECKS
         if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
 #endif
+        if (B.hop_log && g == 0) {
+            const int64_t li = B.hop_log_off[c] + hop;
+            B.hop_log[2 * li] = from;
+            B.hop_log[2 * li + 1] = to;
+            if (B.hop_rates) {
+                B.hop_rates[2 * li] = totf;
+                B.hop_rates[2 * li + 1] = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
+            }
+        }
         KMC_SECTION(4);
         // ---- clock ----
-        const float dt = e1 * __frcp_rn(tot.hi);
+        const float dt = e1 * __frcp_rn(totf);
         const double t_before = t;
         t += static_cast<double>(dt);
         grp.sync();   // every thread is done reading the lists and rates
@@ -996,6 +1232,28 @@ int table_stage_words(const kmc_batch &b, size_t rest)
 }
 
 template <int G, typename Pairs>
+int launch_warp_kernel(const kmc_batch &b, cudaStream_t st, int grid, size_t smem, int rw, int tw)
+{
+    // The register-rich variant when every block of the launch is resident
+    // at once with 16 warps per SM, else the one that fits 24.
+    const int wpb = b.warps_per_block;
+    const int rich_blocks = (16 / wpb) * sm_count();
+    if (grid <= rich_blocks) {
+        static int configured_rich = 0;
+        const int rc = set_smem(warp_engine_kernel<G, Pairs, 2>, smem, configured_rich);
+        if (rc != KMC_OK) return rc;
+        warp_engine_kernel<G, Pairs, 2><<<grid, wpb * 32, smem, st>>>(b, rw, tw);
+    } else {
+        static int configured = 0;
+        const int rc = set_smem(warp_engine_kernel<G, Pairs, 3>, smem, configured);
+        if (rc != KMC_OK) return rc;
+        warp_engine_kernel<G, Pairs, 3><<<grid, wpb * 32, smem, st>>>(b, rw, tw);
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
+}
+
+template <int G, typename Pairs>
 int launch_warp(const kmc_batch &b, cudaStream_t st)
 {
     constexpr int CPW = 32 / G;
@@ -1015,20 +1273,18 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
                     smem, b.max_sites, G, wpb);
     const int grid = (b.n_work + wpb - 1) / wpb;
     if (grid <= 0) return KMC_OK;
-    // The register-rich variant when every block of the launch is resident
-    // at once with 16 warps per SM, else the one that fits 24.
-    const int rich_blocks = (16 / wpb) * sm_count();
-    if (grid <= rich_blocks) {
-        static int configured_rich = 0;
-        const int rc = set_smem(warp_engine_kernel<G, Pairs, 2>, smem, configured_rich);
-        if (rc != KMC_OK) return rc;
-        warp_engine_kernel<G, Pairs, 2><<<grid, wpb * 32, smem, st>>>(b, rw, tw);
-    } else {
-        static int configured = 0;
-        const int rc = set_smem(warp_engine_kernel<G, Pairs, 3>, smem, configured);
-        if (rc != KMC_OK) return rc;
-        warp_engine_kernel<G, Pairs, 3><<<grid, wpb * 32, smem, st>>>(b, rw, tw);
-    }
+    if (tw > 0) return launch_warp_kernel<G, TablePairs<true>>(b, st, grid, smem, rw, tw);
+    return launch_warp_kernel<G, Pairs>(b, st, grid, smem, rw, tw);
+}
+
+template <int T, typename Pairs>
+int launch_block_kernel(const kmc_batch &b, cudaStream_t st, size_t smem, int rw, int tw)
+{
+    static int configured = 0;
+    const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
+    if (rc != KMC_OK) return rc;
+    if (b.n_work <= 0) return KMC_OK;
+    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw, tw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }
@@ -1045,13 +1301,8 @@ int launch_block(const kmc_batch &b, cudaStream_t st)
     if (smem > kSmemBudget)
         return fail(KMC_ERR_INVALID, "engine: %zu bytes of shared memory per chain (max_sites %d) exceeds the block budget",
                     smem, b.max_sites);
-    static int configured = 0;
-    const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
-    if (rc != KMC_OK) return rc;
-    if (b.n_work <= 0) return KMC_OK;
-    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw, tw);
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
+    if (tw > 0) return launch_block_kernel<T, TablePairs<true>>(b, st, smem, rw, tw);
+    return launch_block_kernel<T, Pairs>(b, st, smem, rw, tw);
 }
 
 template <typename Pairs>
@@ -1094,7 +1345,7 @@ int run_batch(const kmc_batch &b, cudaStream_t st)
     if (b.replay && !b.replay_off) return fail(KMC_ERR_INVALID, "engine: replay needs replay_off");
     if (b.pair_mode == KMC_PAIRS_TABLE) {
         if (!b.tab_off || !b.tab_LB) return fail(KMC_ERR_INVALID, "engine: table mode needs tab_off and tab_LB");
-        return dispatch<TablePairs>(b, st);
+        return dispatch<TablePairs<false>>(b, st);
     }
     if (b.pair_mode == KMC_PAIRS_POSITIONS) {
         if (!b.tab_pos || !b.tab_pos_off || !b.tab_coef)

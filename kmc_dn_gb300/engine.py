@@ -352,7 +352,7 @@ class Batch:
                  el_energy=None, occupation=None, hops=None, *, streams=None, seed=0,
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
-                 pair_mode="table"):
+                 pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False):
         self.dev = device(dev)
         d = self.dev
         tables_set = tables if isinstance(tables, TableSet) else None
@@ -426,6 +426,20 @@ class Batch:
             roff = np.concatenate([[0], np.cumsum([r.shape[0] for r in rows])[:-1]]).astype(np.int64)
             self.replay = _dev(np.concatenate(rows), torch.float64, d)
             self.replay_off = _dev(roff, torch.int64, d)
+        # optional per-hop log: (from, to) and (total rate, chosen pair's rate)
+        # of every hop, hops_total entries per chain
+        self.hop_log = self.hop_rates = self.hop_log_off = None
+        if hop_log or hop_rates:
+            ht = np.broadcast_to(np.asarray(hops, np.int64), (n,))
+            self._log_off = np.concatenate([[0], np.cumsum(ht)[:-1]]).astype(np.int64)
+            total = int(ht.sum())
+            self.hop_log = torch.full((max(2 * total, 2),), -1, dtype=torch.int32, device=d)
+            if hop_rates:
+                self.hop_rates = torch.zeros(max(2 * total, 2), dtype=torch.float32, device=d)
+            self.hop_log_off = _dev(self._log_off, torch.int64, d)
+        # debug builds: per chain, hops an FP64 selection would pick differently
+        self.select_mismatch = (torch.zeros(n, dtype=torch.int64, device=d)
+                                if count_select_mismatch else None)
         self.cancel = None            # a CancelWord, or None
         self.time_budget_ns = 0       # per launch and chain; 0: none
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
@@ -476,6 +490,12 @@ class Batch:
         if self.cancel is not None:
             b.cancel = self.cancel.device
         b.time_budget_ns = int(self.time_budget_ns)
+        if self.select_mismatch is not None:
+            b.select_mismatch = self.select_mismatch.data_ptr()
+        if self.hop_log is not None:
+            b.hop_log, b.hop_log_off = self.hop_log.data_ptr(), self.hop_log_off.data_ptr()
+            if self.hop_rates is not None:
+                b.hop_rates = self.hop_rates.data_ptr()
         b.pair_mode = self.pair_mode
         if self.tab_pos is not None:
             b.tab_pos, b.tab_pos_off, b.tab_coef = (self.tab_pos.data_ptr(), self.tab_pos_off.data_ptr(),
@@ -521,6 +541,15 @@ class Batch:
                    hops_done=self.hops_done.cpu().numpy(), n_pairs=self.n_pairs.cpu().numpy())
         out["electrode_occupation"] = [eo[o:o + p] for o, p in zip(self.el_off, self.P_c)]
         out["occupation"] = [occ[o:o + n].astype(bool) for o, n in zip(self.site_off, self.N_c)]
+        if self.select_mismatch is not None:
+            out["select_mismatch"] = self.select_mismatch.cpu().numpy()
+        if self.hop_log is not None:
+            ht = self.hops_total.cpu().numpy()
+            lg = self.hop_log.cpu().numpy()
+            out["hop_log"] = [lg[2 * o:2 * (o + k)].reshape(k, 2) for o, k in zip(self._log_off, ht)]
+            if self.hop_rates is not None:
+                hr = self.hop_rates.cpu().numpy()
+                out["hop_rates"] = [hr[2 * o:2 * (o + k)].reshape(k, 2) for o, k in zip(self._log_off, ht)]
         if self.record:
             ot = self.occ_time.cpu().numpy()
             tr = self.traffic.cpu().numpy()

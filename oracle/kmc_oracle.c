@@ -61,19 +61,79 @@ static int possible(int i, int j, int N, const uint8_t *occ)
     return (!occ[i] || occ[j]) ? 0 : 1;
 }
 
+/* Energies (into se, first N entries) and the row-major cumulative rates
+ * (into cum, S*S entries) of one state, kmc_dopant_networks.py:59-97, every
+ * expression in the reference's operand order.  Returns the total rate. */
+static double numba_state_rates(int N, int P, double nu, double kT, double I_0, double R,
+                                const uint8_t *occupation, const double *distances,
+                                const double *E_constant, const double *transitions_constant,
+                                double *se, double *cum)
+{
+    const int S = N + P;
+    const double mIR = -I_0 * R;   /* -I_0*R, evaluated left to right */
+    const double IR = I_0 * R;
+    for (int i = 0; i < N; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < N; ++j)
+            if (j != i) acc += (double)(1 - occupation[j]) / distances[(size_t)i * S + j];
+        se[i] = E_constant[i];
+        se[i] += mIR * acc;
+    }
+    double run = 0.0;
+    for (int i = 0; i < S; ++i) {
+        for (int j = 0; j < S; ++j) {
+            double t;
+            if (!possible(i, j, N, occupation)) {
+                t = 0.0;
+            } else {
+                double dE;
+                if (i < N && j < N)
+                    dE = se[j] - se[i] - IR / distances[(size_t)i * S + j];
+                else
+                    dE = se[j] - se[i];
+                t = (dE > 0) ? nu * exp(-dE / kT) : nu;
+            }
+            t = transitions_constant[(size_t)i * S + j] * t;
+            size_t k = (size_t)i * S + j;
+            run = (k == 0) ? t : t + run;
+            cum[k] = run;
+        }
+    }
+    return cum[(size_t)S * S - 1];
+}
+
+/* First pair k with cum_k/total >= u (kmc_dopant_networks.py:103-110), and
+ * the distance of u from that pair's two cumulative boundaries as a
+ * fraction of the total rate. */
+static size_t numba_select(const double *cum, size_t SS, double total, double u, double *margin)
+{
+    size_t ev = 0;
+    for (size_t k = 0; k < SS; ++k) {
+        if (cum[k] / total >= u) { ev = k; break; }
+    }
+    if (margin) {
+        const double hi = cum[ev] / total - u;
+        const double lo = u - (ev > 0 ? cum[ev - 1] / total : 0.0);
+        *margin = hi < lo ? hi : lo;
+    }
+    return ev;
+}
+
 /* Returns 0 on success, -1 on bad arguments, -2 on allocation failure.
  * occupation (N, in/out), electrode_occupation (P, in/out) as in the
  * reference; traffic (S*S) and occupations_in_time (N) are accumulated when
- * record != 0 (pass zeroed buffers); hop_log (2*hops), hop_times (hops) and
+ * record != 0 (pass zeroed buffers); hop_log (2*hops), hop_times (hops),
  * margins (hops: distance of the event uniform from the chosen pair's
- * cumulative boundaries, relative to the total rate) are optional. */
+ * cumulative boundaries, relative to the total rate), hop_totals (hops: the
+ * total rate) and hop_rates (hops: the chosen pair's rate) are optional. */
 int oracle_numba_replay(int N, int P, double nu, double kT, double I_0, double R,
                         uint8_t *occupation, const double *distances,
                         const double *E_constant, const double *site_energies_in,
                         const double *transitions_constant, int64_t *electrode_occupation,
                         int64_t hops, int record, const double *uniforms,
                         double *time_out, double *traffic, double *occupations_in_time,
-                        int32_t *hop_log, double *hop_times, double *margins)
+                        int32_t *hop_log, double *hop_times, double *margins,
+                        double *hop_totals, double *hop_rates)
 {
     const int S = N + P;
     if (N < 0 || P < 0 || S <= 0 || hops < 0 || !uniforms || !time_out) return -1;
@@ -82,51 +142,17 @@ int oracle_numba_replay(int N, int P, double nu, double kT, double I_0, double R
     if (!se || !cum) { free(se); free(cum); return -2; }
     memcpy(se, site_energies_in, sizeof(double) * (size_t)S);
     double time = 0.0;
-    const double mIR = -I_0 * R;   /* -I_0*R, evaluated left to right */
-    const double IR = I_0 * R;
     for (int64_t hop = 0; hop < hops; ++hop) {
-        for (int i = 0; i < N; ++i) {
-            double acc = 0.0;
-            for (int j = 0; j < N; ++j)
-                if (j != i) acc += (double)(1 - occupation[j]) / distances[(size_t)i * S + j];
-            se[i] = E_constant[i];
-            se[i] += mIR * acc;
-        }
-        double run = 0.0;
-        for (int i = 0; i < S; ++i) {
-            for (int j = 0; j < S; ++j) {
-                double t;
-                if (!possible(i, j, N, occupation)) {
-                    t = 0.0;
-                } else {
-                    double dE;
-                    if (i < N && j < N)
-                        dE = se[j] - se[i] - IR / distances[(size_t)i * S + j];
-                    else
-                        dE = se[j] - se[i];
-                    t = (dE > 0) ? nu * exp(-dE / kT) : nu;
-                }
-                t = transitions_constant[(size_t)i * S + j] * t;
-                size_t k = (size_t)i * S + j;
-                run = (k == 0) ? t : t + run;
-                cum[k] = run;
-            }
-        }
-        const double total = cum[(size_t)S * S - 1];
+        const double total = numba_state_rates(N, P, nu, kT, I_0, R, occupation, distances, E_constant,
+                                               transitions_constant, se, cum);
         const double scale = 1.0 / total;
         const double u1 = uniforms[2 * hop], u2 = uniforms[2 * hop + 1];
         const double hop_time = -log(1.0 - u1) * scale;
-        size_t ev = 0;
-        for (size_t k = 0; k < (size_t)S * S; ++k) {
-            if (cum[k] / total >= u2) { ev = k; break; }
-        }
-        if (margins) {
-            /* distance of u2 from the two cumulative boundaries of the chosen
-             * pair, as a fraction of the total rate */
-            const double hi = cum[ev] / total - u2;
-            const double lo = u2 - (ev > 0 ? cum[ev - 1] / total : 0.0);
-            margins[hop] = hi < lo ? hi : lo;
-        }
+        double mg = 0.0;
+        const size_t ev = numba_select(cum, (size_t)S * S, total, u2, &mg);
+        if (margins) margins[hop] = mg;
+        if (hop_totals) hop_totals[hop] = total;
+        if (hop_rates) hop_rates[hop] = cum[ev] - (ev > 0 ? cum[ev - 1] : 0.0);
         int from = (int)(ev / (size_t)S), to = (int)(ev % (size_t)S);
         if (from < N) occupation[from] = 0; else electrode_occupation[from - N] -= 1;
         if (to < N) occupation[to] = 1; else electrode_occupation[to - N] += 1;
@@ -143,6 +169,65 @@ int oracle_numba_replay(int N, int P, double nu, double kT, double I_0, double R
     free(se);
     free(cum);
     return 0;
+}
+
+static inline uint64_t splitmix64(uint64_t x);
+
+/* A replay stream on which every hop's event uniform lies at least
+ * min_margin (as a fraction of the total rate) from the cumulative
+ * boundaries of the pair it selects: the numba loop above is run on uniforms
+ * from SplitMix64 (seed), and an event uniform closer than min_margin to a
+ * boundary is replaced by the generator's next value (at most 100000 tries).
+ * Any hop loop whose cumulative rates are within min_margin of the FP64
+ * ones must then follow the FP64 hop sequence on this stream exactly.
+ * occupation (N) is the start state and is not modified; site_energies (S)
+ * carries the electrode energies at [N, S).  uniforms_out gets
+ * 2*hops values in (0,1); *redraws the number of replaced uniforms.
+ * Returns 0, -1 on bad arguments, -2 on allocation failure, -3 when no
+ * clear uniform was found for some hop. */
+int oracle_clear_stream(int N, int P, double nu, double kT, double I_0, double R,
+                        const uint8_t *occupation_in, const double *distances,
+                        const double *E_constant, const double *site_energies_in,
+                        const double *transitions_constant, int64_t hops, uint64_t seed,
+                        double min_margin, double *uniforms_out, int64_t *redraws)
+{
+    const int S = N + P;
+    if (N < 0 || P < 0 || S <= 0 || hops < 0 || !uniforms_out) return -1;
+    double *se = (double *)malloc(sizeof(double) * (size_t)S);
+    double *cum = (double *)malloc(sizeof(double) * (size_t)S * (size_t)S);
+    uint8_t *occ = (uint8_t *)malloc((size_t)(N > 0 ? N : 1));
+    if (!se || !cum || !occ) { free(se); free(cum); free(occ); return -2; }
+    if (N > 0) memcpy(occ, occupation_in, (size_t)N);
+    memcpy(se, site_energies_in, sizeof(double) * (size_t)S);   /* electrode energies at [N, S) */
+    uint64_t ctr = 0;
+    int64_t nre = 0;
+    int rc = 0;
+    const uint64_t golden = 0x9E3779B97F4A7C15ULL;
+    for (int64_t hop = 0; hop < hops && rc == 0; ++hop) {
+        const double total = numba_state_rates(N, P, nu, kT, I_0, R, occ, distances, E_constant,
+                                               transitions_constant, se, cum);
+        const double u1 = ((double)(splitmix64(seed + (++ctr) * golden) >> 11) + 0.5) * 0x1.0p-53;
+        double u2 = 0.0, mg = -1.0;
+        size_t ev = 0;
+        int tries = 0;
+        for (; tries < 100000; ++tries) {
+            u2 = ((double)(splitmix64(seed + (++ctr) * golden) >> 11) + 0.5) * 0x1.0p-53;
+            ev = numba_select(cum, (size_t)S * S, total, u2, &mg);
+            if (mg >= min_margin) break;
+        }
+        if (mg < min_margin) rc = -3;
+        nre += tries;
+        uniforms_out[2 * hop] = u1;
+        uniforms_out[2 * hop + 1] = u2;
+        const int from = (int)(ev / (size_t)S), to = (int)(ev % (size_t)S);
+        if (from < N) occ[from] = 0;
+        if (to < N) occ[to] = 1;
+    }
+    if (redraws) *redraws = nre;
+    free(se);
+    free(cum);
+    free(occ);
+    return rc;
 }
 
 /* ----------------------------------------------------------------------- */

@@ -34,7 +34,11 @@ def lib():
         L.oracle_numba_replay.restype = C.c_int
         L.oracle_numba_replay.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                           C.c_double, _u8p, _dp, _dp, _dp, _dp, _i64p, C.c_int64,
-                                          C.c_int, _dp, _dp, _dp, _dp, _i32p, _dp, _dp]
+                                          C.c_int, _dp, _dp, _dp, _dp, _i32p, _dp, _dp, _dp, _dp]
+        L.oracle_clear_stream.restype = C.c_int
+        L.oracle_clear_stream.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, _u8p, _dp, _dp, _dp, _dp, C.c_int64, C.c_uint64,
+                                          C.c_double, _dp, _i64p]
         L.oracle_go_simulate.restype = C.c_double
         L.oracle_go_simulate.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                          C.c_double, _u8p, _dp, _dp, _dp, _dp, _dp, C.c_int64,
@@ -60,7 +64,9 @@ def numba_replay(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     """FP64 restatement of _simulate_discrete_record with a replay stream.
 
     Returns dict(time, occupation, electrode_occupation, traffic,
-    occupations_in_time, hop_log (hops, 2), hop_times, margins)."""
+    occupations_in_time, hop_log (hops, 2), hop_times, margins, hop_totals
+    (the total rate of each hop's state), hop_rates (the chosen pair's
+    rate))."""
     S = N + P
     hops = len(uniforms) // 2 if hops is None else int(hops)
     occ = np.ascontiguousarray(occupation, dtype=np.uint8).copy()
@@ -76,15 +82,38 @@ def numba_replay(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     log = np.zeros((hops, 2), np.int32)
     ht = np.zeros(hops)
     mg = np.zeros(hops)
+    tot = np.zeros(hops)
+    rch = np.zeros(hops)
     t = C.c_double(0)
     rc = lib().oracle_numba_replay(N, P, nu, kT, I_0, R, _p(occ, _u8p), _p(d, _dp), _p(ec, _dp),
                                    _p(se, _dp), _p(tc, _dp), _p(eo, _i64p), hops, int(record),
                                    _p(u, _dp), C.byref(t), _p(traffic, _dp), _p(oit, _dp),
-                                   _p(log, _i32p), _p(ht, _dp), _p(mg, _dp))
+                                   _p(log, _i32p), _p(ht, _dp), _p(mg, _dp), _p(tot, _dp), _p(rch, _dp))
     if rc != 0:
         raise RuntimeError(f"oracle_numba_replay failed: {rc}")
     return dict(time=t.value, occupation=occ, electrode_occupation=eo, traffic=traffic,
-                occupations_in_time=oit[:N], hop_log=log, hop_times=ht, margins=mg)
+                occupations_in_time=oit[:N], hop_log=log, hop_times=ht, margins=mg,
+                hop_totals=tot, hop_rates=rch)
+
+
+def clear_stream(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
+                 transitions_constant, hops, seed, min_margin=1e-4):
+    """A replay stream (2*hops uniforms) on which every hop of the numba
+    loop started from ``occupation`` selects its pair with the event uniform
+    at least ``min_margin`` of the total rate away from that pair's
+    cumulative boundaries (close uniforms are redrawn).  Returns (uniforms,
+    number of redraws)."""
+    u = np.zeros(2 * int(hops))
+    nre = C.c_int64(0)
+    rc = lib().oracle_clear_stream(
+        N, P, nu, kT, I_0, R, _p(np.ascontiguousarray(occupation, dtype=np.uint8), _u8p),
+        _p(np.ascontiguousarray(distances, np.float64), _dp), _p(np.ascontiguousarray(E_constant, np.float64), _dp),
+        _p(np.ascontiguousarray(site_energies, np.float64), _dp),
+        _p(np.ascontiguousarray(transitions_constant, np.float64), _dp), int(hops),
+        C.c_uint64(int(seed) & (2**64 - 1)), float(min_margin), _p(u, _dp), C.byref(nre))
+    if rc != 0:
+        raise RuntimeError(f"oracle_clear_stream failed: {rc}")
+    return u, nre.value
 
 
 def go_simulate(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
