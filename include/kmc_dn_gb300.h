@@ -223,6 +223,12 @@ typedef struct kmc_batch {
      * FP64 scan and compare over the same FP32 per-thread sums would place
      * on another pair than the engine's exact integer compare; NULL: off */
     unsigned long long *select_mismatch;
+    /* optional, per chain: the largest difference (in units of kT) between
+     * the FP32 energies the O(N) incremental updates carried and the same
+     * energies recomputed from scratch, taken at every re-anchor (every
+     * `reanchor` hops): the drift the periodic re-anchor removes.  Kept as
+     * a running maximum over launches.  NULL: not measured */
+    float *energy_drift;
 } kmc_batch;
 
 /*

@@ -721,12 +721,18 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // lists built from them.  Run at the launch start and at every absolute
     // hop index that is a multiple of `reanchor`, so a run split into
     // launches anchors at the same hops.
-    auto anchor_and_build = [&]() {
+    // With `drift`, the energies the incremental updates carried since the
+    // last anchor are compared with the recomputed ones first, and the
+    // largest difference (in units of kT) is kept per chain.
+    float drift_max = 0.0f;
+    auto anchor_and_build = [&](bool drift) {
         for (int j = g; j < N; j += G) {
             float acc = 0.0f;
             for (int k = 0; k < N; ++k)
                 if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += pairs.coulomb(j, k);
-            sm.E[j] = Ec[j] - acc;
+            const float e = Ec[j] - acc;
+            if (drift) drift_max = fmaxf(drift_max, fabsf(e - sm.E[j]));
+            sm.E[j] = e;
         }
         const int z = N - h;
         int wcur = 0, cum = 0;
@@ -755,7 +761,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         grp.sync();
     };
-    anchor_and_build();
+    anchor_and_build(false);
     int until_anchor = reanchor - static_cast<int>(hop % reanchor);
 
     // Thread g holds the two uniforms of hop rbase + (g mod 32), already
@@ -788,7 +794,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         if (until_anchor == 0) {
             grp.sync();           // bit updates of the last hop are visible
-            anchor_and_build();
+            anchor_and_build(B.energy_drift != nullptr);
             until_anchor = reanchor;
         }
         --until_anchor;
@@ -1118,6 +1124,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     }
     for (int j = g; j < N; j += G) occ_g[j] = static_cast<uint8_t>((sm.occw[j >> 5] >> (j & 31)) & 1u);
     for (int e = g; e < P; e += G) B.electrode_occupation[eoff + e] += sm.eo[e];
+    if (B.energy_drift) {
+        // largest drift of the chain's threads, in kT (non-negative floats
+        // order as their bit patterns)
+        const float dm = __uint_as_float(grp.max_u32(__float_as_uint(drift_max * (cs / kLog2e))));
+        if (g == 0) B.energy_drift[c] = fmaxf(B.energy_drift[c], dm);
+    }
     if (g == 0) {
         B.time[c] = t;
         B.hops_done[c] = hop;

@@ -90,6 +90,7 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
     double *cum = ws + 2 * (size_t)N * N;   // [S*S] rates, then running sums
 
     const int tid = threadIdx.x;
+    const bool kT_is_one = (kT == 1.0);
     const double IR = I0 * R;
     const double mIR = -I0 * R;
     for (int k = tid; k < N * N; k += kThreads) {
@@ -131,7 +132,8 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
                 double dE;
                 if (i < N && j < N) dE = se[j] - se[i] - ird[(size_t)i * N + j];
                 else dE = se[j] - se[i];
-                t = (dE > 0) ? nu * exp(-dE / kT) : nu;
+                // x / 1.0 == x exactly, so kT = 1 skips the division bit-exactly
+                t = (dE > 0) ? nu * exp(kT_is_one ? -dE : -dE / kT) : nu;
             }
             t = tc[k] * t;
             cum[k] = t;
@@ -163,8 +165,15 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
             u1 = u01_from64(r.x, r.y);
             u2 = u01_from64(r.z, r.w);
         }
-        for (int k = kb; k < ke; ++k) {
-            if (cum[k] / total >= u2) { atomicMin(&ev_min, k); break; }
+        // First k with cum_k/total >= u2 (the reference's test, one FP64
+        // division per candidate).  cum is non-decreasing, so only the chunk
+        // whose last entry passes can hold it; a chunk whose last entry is
+        // below u2*total by far more than the rounding of either side (a
+        // relative 1e-12) cannot pass and is skipped without dividing.
+        if (kb < ke && !(cum[ke - 1] < u2 * total * (1.0 - 1.0e-12))) {
+            for (int k = kb; k < ke; ++k) {
+                if (cum[k] / total >= u2) { atomicMin(&ev_min, k); break; }
+            }
         }
         __syncthreads();
         if (tid == 0) {

@@ -352,7 +352,8 @@ class Batch:
                  el_energy=None, occupation=None, hops=None, *, streams=None, seed=0,
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
-                 pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False):
+                 pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False,
+                 measure_drift=False):
         self.dev = device(dev)
         d = self.dev
         tables_set = tables if isinstance(tables, TableSet) else None
@@ -440,6 +441,8 @@ class Batch:
         # debug builds: per chain, hops an FP64 selection would pick differently
         self.select_mismatch = (torch.zeros(n, dtype=torch.int64, device=d)
                                 if count_select_mismatch else None)
+        # per chain: largest incremental-energy drift found at a re-anchor (kT)
+        self.energy_drift = torch.zeros(n, dtype=torch.float32, device=d) if measure_drift else None
         self.cancel = None            # a CancelWord, or None
         self.time_budget_ns = 0       # per launch and chain; 0: none
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
@@ -492,6 +495,8 @@ class Batch:
         b.time_budget_ns = int(self.time_budget_ns)
         if self.select_mismatch is not None:
             b.select_mismatch = self.select_mismatch.data_ptr()
+        if self.energy_drift is not None:
+            b.energy_drift = self.energy_drift.data_ptr()
         if self.hop_log is not None:
             b.hop_log, b.hop_log_off = self.hop_log.data_ptr(), self.hop_log_off.data_ptr()
             if self.hop_rates is not None:
@@ -543,6 +548,8 @@ class Batch:
         out["occupation"] = [occ[o:o + n].astype(bool) for o, n in zip(self.site_off, self.N_c)]
         if self.select_mismatch is not None:
             out["select_mismatch"] = self.select_mismatch.cpu().numpy()
+        if self.energy_drift is not None:
+            out["energy_drift"] = self.energy_drift.cpu().numpy()
         if self.hop_log is not None:
             ht = self.hops_total.cpu().numpy()
             lg = self.hop_log.cpu().numpy()

@@ -25,7 +25,9 @@ seed.  The server
   remaining work is launched first, short requests use high-priority
   streams and wider thread groups, and long requests run in shorter quanta
   so that the blocks a short request waits for free up within a few
-  milliseconds;
+  milliseconds; while a short request waits or runs, long requests get no
+  new quantum at all (strict priority, with a starvation guard), so the
+  short one has the device to itself once the long quanta in flight end;
 * returns per-chain currents, times and electrode counts, and records each
   request's latency (arrival to result on the host).
 
@@ -70,6 +72,7 @@ class Request:
     started: bool = False
     cancel_word: Optional[object] = None   # engine.CancelWord while the request is active
     cancelled: bool = False
+    paused_since: Optional[float] = None   # a long request held back for short ones since
 
 
 def _request_bytes(n_chains, N, P):
@@ -89,6 +92,8 @@ class Server:
     short_hops:     requests with at most this many hops are short
     long_thread_share: fraction of the device's resident-thread slots that
                     long requests may hold (default 0.75)
+    max_long_pause: seconds a long request may be held back while short
+                    requests run (strict priority) before it gets a quantum
     max_active_chains:      resident chains in all
     mem_budget:     bytes of chain state admitted at once (default: a
                     quarter of the free device memory at start)
@@ -99,7 +104,7 @@ class Server:
     def __init__(self, networks, *, quantum=4096, mem_budget=None,
                  pair_mode="positions", lanes=None, dev=None, short_hops=20000,
                  max_active_chains=16384, long_thread_share=0.75, quantum_long=_REANCHOR,
-                 short_lanes_factor=4):
+                 short_lanes_factor=4, max_long_pause=1.0):
         if quantum % _REANCHOR or quantum_long % _REANCHOR or quantum_long <= 0:
             raise ValueError("quantum and quantum_long must be multiples of the re-anchor period (1024)")
         d = torch.device(dev if dev is not None else "cuda")
@@ -111,6 +116,7 @@ class Server:
         self.lanes = lanes
         self.short_lanes_factor = int(short_lanes_factor)
         self.short_hops = int(short_hops)
+        self.max_long_pause = float(max_long_pause)
         free, _total = torch.cuda.mem_get_info(self.dev)
         self.mem_budget = int(mem_budget if mem_budget is not None else free // 4)
         self.mem_used = 0
@@ -294,12 +300,40 @@ class Server:
             self.active_long_threads += self._threads(req)
         self.active.append(req)
 
+    def _short_busy(self):
+        """A short request is waiting, or active with work left to run."""
+        if any(r.hops <= self.short_hops for r in self.queue):
+            return True
+        return any(r.hops <= self.short_hops and r.launched_hops < r.hops and not r.cancelled
+                   for r in self.active)
+
+    def _may_launch(self, req, short_busy, now):
+        """Strict priority for short requests: while one waits or runs, long
+        requests get no new quantum (the quanta in flight end within one
+        quantum, so a short request soon has the device to itself).  A long
+        request paused for more than max_long_pause seconds gets one quantum
+        all the same, so that a steady stream of short requests cannot
+        starve it."""
+        if req.hops <= self.short_hops or not short_busy:
+            req.paused_since = None
+            return True
+        if req.paused_since is None:
+            req.paused_since = now
+        if now - req.paused_since > self.max_long_pause:
+            req.paused_since = None
+            return True
+        return False
+
     def _launch_ready(self):
+        short_busy = self._short_busy()
+        now = time.perf_counter()
         # least remaining work first
         for req in sorted(self.active, key=lambda r: r.hops - r.launched_hops):
             if req.launched_hops >= req.hops or req.cancelled:
                 continue
             if req.inflight is not None and not req.inflight.query():
+                continue
+            if not self._may_launch(req, short_busy, now):
                 continue
             q = self.quantum if req.hops <= self.short_hops else self.quantum_long
             seg = min(q, req.hops - req.launched_hops)
@@ -327,8 +361,14 @@ class Server:
                                 for e, t in zip(r["electrode_occupation"], r["time"])])
                 req.done_at = time.perf_counter()
                 self.hops_done += int(np.sum(r["hops_done"]))
+                status = r["status"].copy()
+                if req.cancelled:
+                    # a cancel that lands between two quanta stops the chains
+                    # before the next launch, which then never polls the
+                    # cancel word: they are cancelled all the same
+                    status[(status == _native.KMC_OK) & (r["hops_done"] < req.hops)] = _native.KMC_ERR_CANCELLED
                 out = dict(currents=cur, time=r["time"], electrode_occupation=np.array(r["electrode_occupation"]),
-                           status=r["status"], latency=req.done_at - req.arrival, cancelled=req.cancelled,
+                           status=status, latency=req.done_at - req.arrival, cancelled=req.cancelled,
                            hops_done=r["hops_done"])
                 self.mem_used -= req.bytes
                 self.active_chains -= req.voltages.shape[0]

@@ -198,3 +198,27 @@ def test_prune_cut_is_taken_in_float32_as_go_does():
     assert p[0, 2] == 0.0 and p[2, 0] == 0.0          # float32(0.1 + 1e-12) == float32(0.1): not above
     assert p[0, 1] == 1.0 and p[1, 2] == 0.25         # clearly above: kept with its FP64 value
     np.testing.assert_array_equal(prune(tc, 0.0), tc)  # no cut: unchanged
+
+
+def test_long_requests_pause_while_short_ones_run():
+    """Strict priority: a long request gets no new quantum while a short one
+    is waiting or active, until the starvation guard lets one through."""
+    from kmc_dn_gb300.serving import Request
+    s, _ = _admission_server(mem_budget=10**12, long_thread_budget=10**9)
+    s.max_long_pause = 0.5
+    long_ = Request(1, np.zeros((64, 8)), 10**6, 1)
+    short = Request(0, np.zeros((32, 8)), 10**4, 2)
+    assert not s._short_busy()
+    assert s._may_launch(long_, s._short_busy(), now=0.0)
+    s.queue.append(short)
+    busy = s._short_busy()
+    assert busy
+    assert s._may_launch(short, busy, now=1.0)             # short ones always launch
+    assert not s._may_launch(long_, busy, now=1.0)          # paused from t = 1.0
+    assert not s._may_launch(long_, busy, now=1.4)
+    assert s._may_launch(long_, busy, now=1.6)              # held back > 0.5 s: one quantum
+    assert not s._may_launch(long_, busy, now=1.7)          # and paused again
+    s.queue.clear()
+    short.launched_hops = short.hops
+    s.active = [short]                                      # short work all launched: not busy
+    assert not s._short_busy() and s._may_launch(long_, False, now=2.0)
