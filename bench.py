@@ -354,6 +354,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--persistent", action="store_true",
+                    help="uneven workload: persistent launches (resident blocks claim work items)")
     ap.add_argument("--workload", default="homogeneous",
                     choices=["homogeneous", "uneven", "large", "serving", "meanfield"],
                     help="homogeneous: the headline line; the others measure the other "
@@ -591,7 +593,10 @@ def run_e2e(net, V, hops, seed, lanes):
             "d2h_bytes_per_step": int(d2h), "api": "kmc_run_batch_host (C ABI, host buffers)"}
 
 
-def _timed_launch(b, hops, streams):
+def _timed_launch(b, hops, streams, bin_ends=None):
+    """One launch per size bin, bin k on streams[k % len(streams)]; the
+    time from the first launch to the end of the last.  bin_ends (one
+    timing event per bin) receive each bin's end, for per-bin times."""
     import torch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -600,12 +605,15 @@ def _timed_launch(b, hops, streams):
     for st in streams:
         st.wait_event(e0)
     b.launch(hops, bin_streams=streams)
-    for st in streams:
-        ev = torch.cuda.Event()
+    for k, st in enumerate(streams):
+        ev = bin_ends[k] if bin_ends else torch.cuda.Event()
         ev.record(st)
         torch.cuda.current_stream().wait_event(ev)
     e1.record()
     e1.synchronize()
+    if bin_ends:
+        for k, ev in enumerate(bin_ends):
+            b._bins[k]["seconds"] = e0.elapsed_time(ev) * 1e-3
     return e0.elapsed_time(e1) * 1e-3
 
 
@@ -631,9 +639,12 @@ def bench_uneven(args):
         tune_s = time.perf_counter() - t0
     b = Batch(specs, np.arange(n), [net.kT for net, _ in nets], [net.E_constant() for net, _ in nets],
               [net.electrodes[:, 3] for net, _ in nets], [net.occupation.astype(np.uint8) for net, _ in nets],
-              hops, seed=args.seed + 5, pair_mode="positions", lanes=lanes)
+              hops, seed=args.seed + 5, pair_mode="positions", lanes=lanes,
+              warps_per_block=(getattr(lanes, "warps", None) or 4) if lanes else 4,
+              persistent=args.persistent)
     streams = [torch.cuda.Stream() for _ in range(len(b._bins))]
-    dt = _timed_launch(b, int(hops.max()), streams)
+    bin_ends = [torch.cuda.Event(enable_timing=True) for _ in b._bins]
+    dt = _timed_launch(b, int(hops.max()), streams, bin_ends)
     r = b.results()
     assert np.all(r["status"] == 0)
     done = int(r["hops_done"].sum())
@@ -641,8 +652,11 @@ def bench_uneven(args):
     bins = []
     for bn in b._bins:
         idx = bn["chains"]
-        bins.append({"lanes_per_chain": bn["G"], "chains": int(len(idx)), "S_range": [int(S[idx].min()), int(S[idx].max())],
-                     "hops": int(r["hops_done"][idx].sum())})
+        bins.append({"lanes_per_chain": bn["G"], "warps_per_block": b._warps(bn["G"]), "chains": int(len(idx)),
+                     "S_range": [int(S[idx].min()), int(S[idx].max())],
+                     "hops": int(r["hops_done"][idx].sum()), "max_hops": int(hops[idx].max()),
+                     "seconds": bn.get("seconds"),
+                     "pairs_per_s": float(r["n_pairs"][idx].sum()) / bn["seconds"] if bn.get("seconds") else None})
     if not args.no_accuracy:
         # FP32 vs FP64 currents per size bin: two networks of each bin, 32
         # replicas each on both kernels (fewer hops for the large bins: the
@@ -661,6 +675,8 @@ def bench_uneven(args):
                                    "hops log-uniform [1e4,1e6]", "n_chains": n, "total_hops": done,
                        "pair_mode": "positions", "bins": bins, "host_setup_s": setup_s,
                        "lanes": "autotuned per size class" if lanes else "default by size",
+                       "launch": "persistent (work claimed with an atomic counter)" if args.persistent
+                                 else "one work item per warp",
                        "autotune_s": tune_s,
                        "autotuned": {str(k): v for k, v in getattr(lanes, "picked", {}).items()}},
             "gpu_launches": len(b._bins), "n_pairs_per_s": float(r["n_pairs"].sum()) / dt}

@@ -229,6 +229,12 @@ typedef struct kmc_batch {
      * `reanchor` hops): the drift the periodic re-anchor removes.  Kept as
      * a running maximum over launches.  NULL: not measured */
     float *energy_drift;
+    /* optional: a device counter, zero at launch, that makes the launch
+     * persistent -- as many blocks as stay resident, each warp (warp slices)
+     * or block (block groups) claiming the next work item with an atomic
+     * add when its chains are done, instead of one item per warp for the
+     * whole launch.  Results do not depend on it.  NULL: static launch */
+    int32_t *work_counter;
 } kmc_batch;
 
 /*

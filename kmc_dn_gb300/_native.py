@@ -63,7 +63,7 @@ class KmcBatch(C.Structure):
         ("pair_mode", _i32), ("tab_pos", _vp), ("tab_pos_off", _vp), ("tab_coef", _vp),
         ("time_budget_ns", _i64),
         ("hop_log", _vp), ("hop_rates", _vp), ("hop_log_off", _vp), ("select_mismatch", _vp),
-        ("energy_drift", _vp),
+        ("energy_drift", _vp), ("work_counter", _vp),
     ]
 
 

@@ -7,7 +7,8 @@ up to 256 sites, block groups 64..512 from 48 sites) and warps per block in
 the fastest (hops/s).  Results are cached per (GPU name, size class, number of
 chains) in a JSON file (``KMC_DN_AUTOTUNE_CACHE`` or
 ``~/.cache/kmc_dn_gb300/autotune.json``), so a workload is tuned once per
-machine.  ``choose`` returns a ``lanes`` callable for ``Batch``.
+machine.  ``choose`` returns a ``lanes`` callable for ``Batch`` whose
+``warps`` attribute maps each picked width to its warps per block.
 """
 from __future__ import annotations
 
@@ -73,10 +74,13 @@ def _candidates(S):
     return c
 
 
-def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pair_mode="table"):
+def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pair_mode="table", repeats=3):
     """Time every candidate (G, warps per block) for n_chains chains of S
-    sites (CUDA events around one launch after a warm-up launch); return the
-    best as dict(G, warps_per_block, hops_per_s, table)."""
+    sites (CUDA events around ``repeats`` launches after a warm-up launch,
+    the median kept, so one slow launch does not move the pick); return the
+    best as dict(G, warps_per_block, hops_per_s, hop_latency_s, table).
+    hop_latency_s is the launch time per hop, the per-hop latency of a chain
+    at the class's chain count."""
     import torch
     from . import workloads
     from .engine import Batch, TableSpec
@@ -101,18 +105,23 @@ def tune_size_class(S, n_chains, hops=2048, seed=0, dev=None, verbose=False, pai
                 b.launch(1024)
             except KmcError:            # the shape does not fit (shared memory): not a candidate
                 continue
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            b.launch(hops)
-            e1.record()
-            e1.synchronize()
-            rate = n_chains * hops / (e0.elapsed_time(e1) * 1e-3)
-            table.append((G, W, rate))
+            ts = []
+            for _ in range(repeats):
+                b.hops_done.zero_()          # each timed launch runs the same hops again
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                b.launch(hops)
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) * 1e-3)
+            t = float(np.median(ts))
+            rate = n_chains * hops / t
+            table.append((G, W, rate, t / hops))
             if verbose:
-                print(f"S={S} C={n_chains} G={G} W={W}: {rate:.3e} hops/s")
-    G, W, rate = max(table, key=lambda r: r[2])
-    return dict(G=int(G), warps_per_block=int(W), hops_per_s=float(rate),
+                print(f"S={S} C={n_chains} G={G} W={W}: {rate:.3e} hops/s, {t / hops * 1e6:.2f} us/hop")
+    G, W, rate, lat = max(table, key=lambda r: r[2])
+    return dict(G=int(G), warps_per_block=int(W), hops_per_s=float(rate), hop_latency_s=float(lat),
                 table=[list(map(float, r)) for r in table])
 
 
@@ -133,11 +142,17 @@ def choose(S_values, n_chains=None, dev=None, tune=True, pair_mode="table", max_
             if k not in cache and tune:
                 cache[k] = tune_size_class(sc, nc, dev=dev, pair_mode=pair_mode)
                 _save(cache)
-            picked[sc] = cache[k]["G"] if k in cache else None
+            picked[sc] = (cache[k]["G"], cache[k].get("warps_per_block", 4)) if k in cache else None
     from .engine import default_lanes
 
     def lanes(S):
         g = picked.get(size_class(S))
-        return g if g else default_lanes(S)
-    lanes.picked = picked
+        return g[0] if g else default_lanes(S)
+    # warps per block for each picked width (Batch(warps_per_block=...))
+    warps = {}
+    for g in picked.values():
+        if g and g[0] <= 32:
+            warps[g[0]] = max(warps.get(g[0], 0), g[1])
+    lanes.picked = {sc: (g[0] if g else None) for sc, g in picked.items()}
+    lanes.warps = warps
     return lanes

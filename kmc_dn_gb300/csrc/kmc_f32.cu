@@ -938,7 +938,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (L < 0) L = (A - 1) / M;
         // what remains of u*total beyond the runs before L, back in FP32
         float rem = grp.bcast(from_fixed(target - excl, emax, kShift), L);
-#endif        KMC_SECTION(3);
+#endif
+        KMC_SECTION(3);
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
@@ -1170,14 +1171,33 @@ __global__ void __launch_bounds__(256, MinBlocks) warp_engine_kernel(const kmc_b
     WarpGroup<G> grp;
     grp.init();
     const int warp = threadIdx.x >> 5;
-    const int item = blockIdx.x * B.warps_per_block + warp;
-    if (item >= B.n_work) return;
-    const int c = B.work[item * CPW + grp.sub];
-    if (c < 0 || c >= B.n_chains) return;   // the whole group leaves together
     using Rec = typename Pairs::Rec;
     const int words = chain_list_words<Rec>(B.max_sites) + rate_words;
     ChainSmem<Rec> sm = carve<Rec>(smem + table_words + (warp * CPW + grp.sub) * words, B.max_sites,
                                    rate_words);
+    if (B.work_counter) {
+        // Persistent launch: each warp claims the next unclaimed item when
+        // the chains of its last one are done, so a warp whose chains end
+        // early takes more work instead of idling until its block ends.
+        // Every lane of the warp takes part in each claim (an item with an
+        // empty slot leaves that group idle until the next claim), and the
+        // loop ends for the whole warp at once, when the list is used up.
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            int item = 0;
+            if (lane == 0) item = atomicAdd(B.work_counter, 1);
+            item = __shfl_sync(0xffffffffu, item, 0);
+            if (item >= B.n_work) break;
+            const int c = B.work[item * CPW + grp.sub];
+            if (c >= 0 && c < B.n_chains) run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c, stab);
+            __syncwarp();
+        }
+        return;
+    }
+    const int item = blockIdx.x * B.warps_per_block + warp;
+    if (item >= B.n_work) return;
+    const int c = B.work[item * CPW + grp.sub];
+    if (c < 0 || c >= B.n_chains) return;   // the whole group leaves together
     run_chain<WarpGroup<G>, Pairs>(B, grp, sm, c, stab);
 }
 
@@ -1194,10 +1214,25 @@ __global__ void __launch_bounds__(T) block_engine_kernel(const kmc_batch B, int 
     grp.init();
     grp.sd = scratch;
     grp.si = iscratch;
-    const int c = B.work[blockIdx.x];
-    if (c < 0 || c >= B.n_chains) return;   // uniform over the block
     using Rec = typename Pairs::Rec;
     ChainSmem<Rec> sm = carve<Rec>(smem + table_words, B.max_sites, rate_words);
+    if (B.work_counter) {
+        // Persistent launch: the block claims the next chain when its last
+        // one is done.
+        for (;;) {
+            if (threadIdx.x == 0) iscratch[0] = atomicAdd(B.work_counter, 1);
+            __syncthreads();
+            const int item = iscratch[0];
+            __syncthreads();
+            if (item >= B.n_work) break;
+            const int c = B.work[item];
+            if (c >= 0 && c < B.n_chains) run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c, stab);
+            __syncthreads();
+        }
+        return;
+    }
+    const int c = B.work[blockIdx.x];
+    if (c < 0 || c >= B.n_chains) return;   // uniform over the block
     run_chain<BlockGroup<T>, Pairs>(B, grp, sm, c, stab);
 }
 
@@ -1250,6 +1285,21 @@ int launch_warp_kernel(const kmc_batch &b, cudaStream_t st, int grid, size_t sme
     // at once with 16 warps per SM, else the one that fits 24.
     const int wpb = b.warps_per_block;
     const int rich_blocks = (16 / wpb) * sm_count();
+    if (b.work_counter) {
+        // persistent: as many blocks as stay resident at once (85-register
+        // variant), no more than the work needs
+        static int configured_p = 0;
+        const int rc = set_smem(warp_engine_kernel<G, Pairs, 3>, smem, configured_p);
+        if (rc != KMC_OK) return rc;
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_engine_kernel<G, Pairs, 3>,
+                                                                      wpb * 32, smem);
+        if (e != cudaSuccess) return fail_cuda(e, "engine occupancy");
+        const int pgrid = min(grid, max(1, per_sm) * sm_count());
+        warp_engine_kernel<G, Pairs, 3><<<pgrid, wpb * 32, smem, st>>>(b, rw, tw);
+        e = cudaGetLastError();
+        return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
+    }
     if (grid <= rich_blocks) {
         static int configured_rich = 0;
         const int rc = set_smem(warp_engine_kernel<G, Pairs, 2>, smem, configured_rich);
@@ -1296,7 +1346,14 @@ int launch_block_kernel(const kmc_batch &b, cudaStream_t st, size_t smem, int rw
     const int rc = set_smem(block_engine_kernel<T, Pairs>, smem, configured);
     if (rc != KMC_OK) return rc;
     if (b.n_work <= 0) return KMC_OK;
-    block_engine_kernel<T, Pairs><<<b.n_work, T, smem, st>>>(b, rw, tw);
+    int grid = b.n_work;
+    if (b.work_counter) {   // persistent: the resident blocks claim the chains
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, block_engine_kernel<T, Pairs>, T, smem);
+        if (e != cudaSuccess) return fail_cuda(e, "engine occupancy");
+        grid = min(grid, max(1, per_sm) * sm_count());
+    }
+    block_engine_kernel<T, Pairs><<<grid, T, smem, st>>>(b, rw, tw);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }

@@ -353,7 +353,7 @@ class Batch:
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
                  pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False,
-                 measure_drift=False):
+                 measure_drift=False, persistent=False):
         self.dev = device(dev)
         d = self.dev
         tables_set = tables if isinstance(tables, TableSet) else None
@@ -371,7 +371,10 @@ class Batch:
         self.record = int(record)
         self.seed = int(seed) & (2**64 - 1)
         self.reanchor = int(reanchor)
-        self.warps_per_block = int(warps_per_block)
+        # warps per block of the warp-slice launches: one value, or per lanes
+        # width (a dict G -> warps, or a callable G -> warps, as the
+        # autotuner returns it)
+        self.warps_per_block = warps_per_block
 
         ts = tables_set if tables_set is not None else TableSet(self.tables, pair_mode=pair_mode, dev=d)
         self.table_set = ts
@@ -446,6 +449,18 @@ class Batch:
         self.cancel = None            # a CancelWord, or None
         self.time_budget_ns = 0       # per launch and chain; 0: none
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
+        # persistent launches: one work counter per bin, zeroed before each launch
+        self.persistent = bool(persistent)
+        self._counters = (torch.zeros(max(len(self._bins), 1), dtype=torch.int32, device=d)
+                          if self.persistent else None)
+
+    def _warps(self, G):
+        w = self.warps_per_block
+        if callable(w):
+            w = w(G)
+        elif isinstance(w, dict):
+            w = w.get(G, 4)
+        return int(w) if w else 4
 
     # -- work lists --------------------------------------------------------
     def _make_bins(self, lanes, hops):
@@ -485,7 +500,7 @@ class Batch:
         b.n_work = bin_["n_work"]
         b.record = self.record
         b.reanchor = self.reanchor
-        b.warps_per_block = self.warps_per_block
+        b.warps_per_block = self._warps(bin_["G"])
         b.max_hops_per_launch = int(seg)
         b.seed = self.seed
         if self.replay is not None:
@@ -520,6 +535,11 @@ class Batch:
         for i, bin_ in enumerate(self._bins):
             st = bin_streams[i % len(bin_streams)] if bin_streams else stream
             b = self._struct(bin_, seg)
+            if self._counters is not None:
+                ctr = self._counters[i:i + 1]
+                with torch.cuda.stream(st if st is not None else torch.cuda.current_stream()):
+                    ctr.zero_()
+                b.work_counter = ctr.data_ptr()
             check(L.kmc_run_batch(C.byref(b), _stream_handle(st)))
         return self
 

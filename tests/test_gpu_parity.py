@@ -400,3 +400,37 @@ def test_run_batch_host_bins_ragged_batches_like_python_batch(engine_lib):
     np.testing.assert_array_equal(t_out, r["time"])
     np.testing.assert_array_equal(eo, np.concatenate(r["electrode_occupation"]))
     np.testing.assert_array_equal(occ.astype(bool), np.concatenate(r["occupation"]))
+
+
+@pytest.mark.parametrize("pair_mode", ["table", "positions"])
+def test_persistent_launch_gives_the_static_launch_results(engine_lib, pair_mode):
+    """The persistent launch (resident blocks claiming work items with an
+    atomic counter) runs every chain exactly as the one-item-per-warp launch
+    does: bit-identical results on a ragged batch with warp and block groups,
+    also when the run is split into several launches."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    nets = workloads.uneven_batch(600, seed=21, hops_range=(1000, 8000))
+    hops = np.array([h for _, h in nets], np.int64)
+    specs = [TableSpec.from_network(n) if pair_mode == "positions" else
+             TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant) for n, _ in nets]
+
+    def run(persistent, seg=None):
+        b = Batch(specs, np.arange(len(nets)), [n.kT for n, _ in nets], [n.E_constant() for n, _ in nets],
+                  [n.electrodes[:, 3] for n, _ in nets], [n.occupation.astype(np.uint8) for n, _ in nets], hops,
+                  seed=13, pair_mode=pair_mode, lanes=lambda S: 16 if S <= 48 else 32 if S <= 128 else 128,
+                  persistent=persistent, record=2)
+        if seg is None:
+            b.run()
+        else:
+            for _ in range(int(np.ceil(hops.max() / seg))):
+                b.launch(seg)
+        return b.results()
+    a, p, q = run(False), run(True), run(True, seg=2048)
+    assert np.all(a["status"] == 0)
+    for r in (p, q):
+        np.testing.assert_array_equal(a["time"], r["time"])
+        np.testing.assert_array_equal(a["hops_done"], r["hops_done"])
+        for k in ("electrode_occupation", "occupation", "traffic", "occ_time"):
+            for x, y in zip(a[k], r[k]):
+                np.testing.assert_array_equal(x, y)

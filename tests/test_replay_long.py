@@ -18,11 +18,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 MARGIN = 1e-4
-# rate-level tolerances on the replay path: the FP32 total rate within 1e-4
-# of the FP64 one, the chosen pair's probability (its rate / total) within
-# 1e-3 (both far below the 1 % current criterion)
-TOTAL_RTOL = 1e-4
-PROB_RTOL = 1e-3
+# Rate-level tolerances on the replay path, per network size: the FP32 total
+# rate and the chosen pair's probability (its rate / total) against the FP64
+# ones.  What sets them is the FP32 site energies (values of a few hundred kT
+# carried by incremental updates between re-anchors: an energy error dE
+# changes a rate by a relative dE/kT), so they grow with N; all stay well
+# below the 1 % current criterion.
+TOLERANCES = {30: dict(total=1e-4, prob=1e-3), 300: dict(total=2e-3, prob=5e-3)}
 
 
 def _network(N):
@@ -58,6 +60,7 @@ def _engine(net, u, hops, lanes, pair_mode):
 
 
 def _check(net, o, r, hops, label):
+    tol = TOLERANCES[net.N]
     assert r["status"][0] == 0
     log = r["hop_log"][0]
     mism = np.flatnonzero(np.any(log != o["hop_log"], axis=1))
@@ -70,9 +73,9 @@ def _check(net, o, r, hops, label):
     p32 = rates[:, 1] / rates[:, 0]
     p64 = o["hop_rates"] / o["hop_totals"]
     prob_err = np.abs(p32 / p64 - 1.0)
-    assert tot_err.max() <= TOTAL_RTOL, (label, float(tot_err.max()))
-    assert prob_err.max() <= PROB_RTOL, (label, float(prob_err.max()))
-    assert abs(r["time"][0] / o["time"] - 1.0) <= TOTAL_RTOL
+    assert tot_err.max() <= tol["total"], (label, float(tot_err.max()), float(prob_err.max()))
+    assert prob_err.max() <= tol["prob"], (label, float(tot_err.max()), float(prob_err.max()))
+    assert abs(r["time"][0] / o["time"] - 1.0) <= tol["total"]
     return float(tot_err.max()), float(prob_err.max())
 
 
