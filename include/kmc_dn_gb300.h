@@ -83,6 +83,74 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
                      void *workspace, size_t workspace_bytes, void *stream);
 
 /*
+ * kmc_simulate_f64 that also accumulates, into flux_time (P device doubles,
+ * at most 64 electrodes), the time integral of each electrode's expected
+ * net hole inflow: in every state, column N+e minus row N+e of the FP64 rate
+ * matrix, times the hop's time.  electrode_occupation minus flux_time is a
+ * zero-mean martingale, so flux_time / time is a low-variance companion
+ * estimate of the current, used to compare precisions.  The hop sequence is
+ * that of kmc_simulate_f64.  No reference counterpart (measurement support
+ * for the loop kmc_dopant_networks.py:33-135).
+ */
+int kmc_simulate_f64_flux(int32_t n_acceptors, int32_t n_electrodes, double nu, double kT,
+                          double I_0, double R, uint8_t *occupation, const double *distances,
+                          const double *E_constant, const double *site_energies,
+                          const double *transitions_constant, int64_t *electrode_occupation,
+                          int64_t hops, int32_t record, double *traffic,
+                          double *occupations_in_time, const double *uniforms, uint64_t seed,
+                          int32_t *hop_log, double *time_out, int32_t *status_out,
+                          void *workspace, size_t workspace_bytes, void *stream,
+                          double *flux_time);
+
+/*
+ * Many independent plain FP64 chains in one launch (one thread block per
+ * chain), for FP64 statistics beside the batched FP32 engine: each chain is
+ * kmc_simulate_f64 in Philox mode (its own seed, no replay, no hop log).
+ * Every pointer is device memory; per-chain segments are given by offsets:
+ *   pair_off[c]   S*S block of distances / transitions_constant (shareable),
+ *   site_off[c]   N entries of E_constant, occupation (in/out) and, with
+ *                 record, occupations_in_time (accumulated),
+ *   se_off[c]     S entries of site_energies (electrode energies at [N, S)),
+ *   el_off[c]     P entries of electrode_occupation (accumulated) and of
+ *                 flux_time (optional, accumulated; at most 64 electrodes),
+ *   traffic_off[c] S*S block of traffic (record only, accumulated).
+ * time_out[c] and status_out[c] (KMC_OK, KMC_ERR_NONFINITE, or
+ * KMC_ERR_INVALID for a chain whose sizes exceed max_sites) are written.
+ * The workspace holds kmc_simulate_f64_batch_workspace_size(n_chains,
+ * max_sites) bytes.  Replaces running the reference's numba loop once per
+ * chain (kmc_dopant_networks.py:33-135).
+ */
+typedef struct kmc_f64_batch {
+    int32_t n_chains;
+    int32_t max_sites;              /* >= N + P of every chain                 */
+    int32_t record;                 /* 0 / 1 (numba convention)                */
+    const int32_t *N, *P;
+    const double *nu, *kT, *I_0, *R;
+    const int64_t *pair_off;
+    const double *distances, *transitions_constant;
+    const int64_t *site_off;
+    const double *E_constant;
+    const int64_t *se_off;
+    const double *site_energies;
+    uint8_t *occupation;
+    const int64_t *el_off;
+    int64_t *electrode_occupation;
+    const int64_t *hops;
+    const uint64_t *seeds;
+    const int64_t *traffic_off;
+    double *traffic;
+    double *occupations_in_time;
+    double *time_out;
+    int32_t *status_out;
+    double *flux_time;              /* optional                                */
+    double *workspace;
+    size_t workspace_bytes;
+} kmc_f64_batch;
+
+size_t kmc_simulate_f64_batch_workspace_size(int32_t n_chains, int32_t max_sites);
+int kmc_simulate_f64_batch(const kmc_f64_batch *batch, void *stream);
+
+/*
  * kmc_simulate_f64 without a workspace argument, for callers that cannot
  * allocate device memory at the point of the call: a host application that
  * owns the device through its own memory pool and passes this library only
@@ -235,6 +303,13 @@ typedef struct kmc_batch {
      * add when its chains are done, instead of one item per warp for the
      * whole launch.  Results do not depend on it.  NULL: static launch */
     int32_t *work_counter;
+    /* optional, electrode pool (P doubles per chain), accumulated: the time
+     * integral of each electrode's expected net inflow J_e = sum over holes
+     * of rate(i -> e) - sum over empty acceptors of rate(e -> j), taken in
+     * every state for the time spent in it.  electrode_occupation minus this
+     * is a zero-mean martingale, so it is a low-variance companion estimate
+     * of the current (accuracy checks).  NULL: not computed */
+    double *flux_time;
 } kmc_batch;
 
 /*

@@ -14,7 +14,7 @@ __all__ = ["lib", "check", "KmcError", "NativeLibraryError", "KmcBatch", "LIB_PA
            "KMC_OK", "KMC_ERR_INVALID", "KMC_ERR_CUDA", "KMC_ERR_OOM", "KMC_ERR_TIMEOUT",
            "KMC_ERR_NONFINITE", "KMC_ERR_CANCELLED", "RECORD_NONE", "RECORD_NUMBA", "RECORD_GO",
            "PAIRS_TABLE", "PAIRS_POSITIONS",
-           "EXPORTED", "KmcMfBatch", "MF_RATES_F64", "MF_RATES_F32"]
+           "EXPORTED", "KmcMfBatch", "KmcF64Batch", "MF_RATES_F64", "MF_RATES_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 # KMC_DN_GB300_LIB selects another build of the same ABI (the debug-checks or
@@ -63,7 +63,21 @@ class KmcBatch(C.Structure):
         ("pair_mode", _i32), ("tab_pos", _vp), ("tab_pos_off", _vp), ("tab_coef", _vp),
         ("time_budget_ns", _i64),
         ("hop_log", _vp), ("hop_rates", _vp), ("hop_log_off", _vp), ("select_mismatch", _vp),
-        ("energy_drift", _vp), ("work_counter", _vp),
+        ("energy_drift", _vp), ("work_counter", _vp), ("flux_time", _vp),
+    ]
+
+
+class KmcF64Batch(C.Structure):
+    """Mirror of ``struct kmc_f64_batch`` (device addresses)."""
+    _fields_ = [
+        ("n_chains", _i32), ("max_sites", _i32), ("record", _i32),
+        ("N", _vp), ("P", _vp), ("nu", _vp), ("kT", _vp), ("I_0", _vp), ("R", _vp),
+        ("pair_off", _vp), ("distances", _vp), ("transitions_constant", _vp),
+        ("site_off", _vp), ("E_constant", _vp), ("se_off", _vp), ("site_energies", _vp),
+        ("occupation", _vp), ("el_off", _vp), ("electrode_occupation", _vp), ("hops", _vp),
+        ("seeds", _vp), ("traffic_off", _vp), ("traffic", _vp), ("occupations_in_time", _vp),
+        ("time_out", _vp), ("status_out", _vp), ("flux_time", _vp), ("workspace", _vp),
+        ("workspace_bytes", _sz),
     ]
 
 
@@ -88,6 +102,10 @@ _SIGS = {
     "kmc_simulate_f64_workspace_size": (_sz, [_i32]),
     "kmc_simulate_f64": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
                                    _i64, _i32, _vp, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "kmc_simulate_f64_flux": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
+                                        _i64, _i32, _vp, _vp, _vp, _u64, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "kmc_simulate_f64_batch_workspace_size": (_sz, [_i32, _i32]),
+    "kmc_simulate_f64_batch": (C.c_int, [C.POINTER(KmcF64Batch), _vp]),
     "kmc_simulate_f64_static": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp,
                                           _vp, _i64, _i32, _vp, _vp, _vp, _u64, _vp, _vp, _vp, _vp]),
     "kmc_build_table": (C.c_int, [_i32, _i32, _f64, _f64, _f64, _vp, _vp, _vp, _vp]),

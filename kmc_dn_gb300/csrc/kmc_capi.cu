@@ -489,6 +489,34 @@ int kmc_simulate_f64(int32_t n_acceptors, int32_t n_electrodes, double nu, doubl
                         static_cast<cudaStream_t>(stream));
 }
 
+size_t kmc_simulate_f64_batch_workspace_size(int32_t n_chains, int32_t max_sites)
+{
+    return (n_chains > 0 && max_sites > 0) ? f64_batch_workspace_size(n_chains, max_sites) : 0;
+}
+
+int kmc_simulate_f64_batch(const kmc_f64_batch *batch, void *stream)
+{
+    if (!batch) return fail(KMC_ERR_INVALID, "kmc_simulate_f64_batch: NULL batch");
+    return simulate_f64_batch(*batch, static_cast<cudaStream_t>(stream));
+}
+
+int kmc_simulate_f64_flux(int32_t n_acceptors, int32_t n_electrodes, double nu, double kT, double I_0,
+                          double R, uint8_t *occupation, const double *distances,
+                          const double *E_constant, const double *site_energies,
+                          const double *transitions_constant, int64_t *electrode_occupation,
+                          int64_t hops, int32_t record, double *traffic, double *occupations_in_time,
+                          const double *uniforms, uint64_t seed, int32_t *hop_log, double *time_out,
+                          int32_t *status_out, void *workspace, size_t workspace_bytes, void *stream,
+                          double *flux_time)
+{
+    if (!flux_time) return fail(KMC_ERR_INVALID, "kmc_simulate_f64_flux: flux_time is NULL");
+    return simulate_f64(n_acceptors, n_electrodes, nu, kT, I_0, R, occupation, distances,
+                        E_constant, site_energies, transitions_constant, electrode_occupation,
+                        hops, record, traffic, occupations_in_time, uniforms, seed, hop_log,
+                        time_out, status_out, workspace, workspace_bytes,
+                        static_cast<cudaStream_t>(stream), flux_time);
+}
+
 int kmc_build_table(int32_t n_acceptors, int32_t n_electrodes, double nu, double I_0, double R,
                     const double *distances, const double *transitions_constant, float *tab_LB,
                     void *stream)

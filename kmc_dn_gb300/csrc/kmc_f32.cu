@@ -203,10 +203,17 @@ __device__ __forceinline__ uint64_t to_fixed(float v, int emax, int shift)
     return sh >= 0 ? (m << sh) : (sh > -24 ? (m >> -sh) : 0ull);
 }
 
-// An integer on that scale back to FP32.
+// An integer on that scale back to FP32: x * 2^(emax - 150 - shift), as
+// (x * 2^-64) * 2^(emax - 86 - shift), both factors exact powers of two in
+// range (x < 2^62, and the second's biased exponent emax + 41 - shift lies
+// in [5, 254] for finite sums).  x itself goes through its two 32-bit halves
+// (within one FP32 ulp).
 __device__ __forceinline__ float from_fixed(uint64_t x, int emax, int shift)
 {
-    return ldexpf(__ull2float_rn(x), emax - 150 - shift);
+    const float f = fmaf(__uint2float_rn(static_cast<uint32_t>(x >> 32)), 4294967296.0f,
+                         __uint2float_rn(static_cast<uint32_t>(x)));
+    const int e = min(emax + 41 - shift, 254);
+    return (f * 0x1.0p-64f) * __int_as_float(e << 23);
 }
 
 // The first cumulative value that reaches u * total, u = uq * 2^-64: the
@@ -379,6 +386,12 @@ struct WarpGroup {
         return F2{__shfl_sync(mask, v.hi, src, G), __shfl_sync(mask, v.lo, src, G)};
     }
     __device__ __forceinline__ uint32_t max_u32(uint32_t v) const { return __reduce_max_sync(mask, v); }
+    __device__ __forceinline__ float sumf(float v) const
+    {
+#pragma unroll
+        for (int d = G / 2; d >= 1; d >>= 1) v += __shfl_xor_sync(mask, v, d, G);
+        return v;
+    }
 #ifdef KMC_DEBUG_CHECKS
     // FP64 inclusive scan (debug builds: the cross-check of the selection)
     __device__ double scan_f64(double v, double &excl, double &tot) const
@@ -510,6 +523,12 @@ struct BlockGroup {
         return x;
     }
 #endif
+    __device__ float sumf(float v) const
+    {
+        float tot;
+        scanf(v, tot);
+        return tot;
+    }
     __device__ uint32_t max_u32(uint32_t v) const
     {
         const uint32_t w = __reduce_max_sync(0xffffffffu, v);
@@ -725,6 +744,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // last anchor are compared with the recomputed ones first, and the
     // largest difference (in units of kT) is kept per chain.
     float drift_max = 0.0f;
+    // The record of electrode g (thread g < P), the same every hop of the
+    // launch: the rebuilds after a hop copy it instead of reading the
+    // electrode's energy from global memory again.
+    Rec el_rec{};
     auto anchor_and_build = [&](bool drift) {
         for (int j = g; j < N; j += G) {
             float acc = 0.0f;
@@ -752,6 +775,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         for (int e = g; e < P; e += G) {
             const Rec r = pairs.rec(N + e, cs * Vel[e]);
+            if (e == g) el_rec = r;   // kept for the list rebuilds of later hops
             sm.src[h + e] = r;
             sm.tgt[z + e] = r;
             if (!Pairs::kSiteInRec) {
@@ -1036,9 +1060,25 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         }
         KMC_SECTION(4);
         // ---- clock ----
-        const float dt = e1 * __frcp_rn(totf);
+        const float dt = e1 * rcp_approx(totf);
         const double t_before = t;
         t += static_cast<double>(dt);
+        if (B.flux_time) {
+            // Expected net hole flow into each electrode in this state,
+            // J_e = sum_holes rate(i -> e) - sum_empty rate(e -> j), times
+            // the time spent in it: the integral of J_e over the run is the
+            // compensator of the electrode's hop count (their difference is
+            // a zero-mean martingale), a low-variance companion estimate of
+            // the current for accuracy checks.
+            for (int e = 0; e < P; ++e) {
+                const Rec er = sm.src[h + e];
+                float part = 0.0f;
+                for (int k = g; k < N; k += G)
+                    part += (k < h) ? pairs.rate(sm.src[k], er, false, cs) : -pairs.rate(er, sm.tgt[k - h], false, cs);
+                const float J = grp.sumf(part);
+                if (g == 0) B.flux_time[eoff + e] += static_cast<double>(J) * static_cast<double>(dt);
+            }
+        }
         grp.sync();   // every thread is done reading the lists and rates
         KMC_SECTION(5);
         // ---- apply the hop and rebuild the lists in one pass ----
@@ -1076,7 +1116,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             }
             if (h_new != h) {
                 for (int e = g; e < P; e += G) {
-                    const Rec r = pairs.rec(N + e, cs * Vel[e]);
+                    const Rec r = (e == g) ? el_rec : pairs.rec(N + e, cs * Vel[e]);
                     sm.src[h_new + e] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[h_new + e] = N + e;
                     sm.tgt[z_new + e] = r;

@@ -70,11 +70,12 @@ __device__ double block_exclusive_scan(double v, double *sh, double &total)
     return warp_base + x - v;
 }
 
-__global__ void __launch_bounds__(kThreads) f64_chain_kernel(
+// One chain run by the whole block (the body of both kernels below).
+__device__ __forceinline__ void f64_chain(
     int N, int P, double nu, double kT, double I0, double R, uint8_t *occ_g, const double *d,
     const double *Ec, const double *se_in, const double *tc, int64_t *eo, int64_t hops,
     int record, double *traffic, double *oit, const double *uniforms, uint64_t seed,
-    int32_t *hop_log, double *time_out, int32_t *status_out, double *ws)
+    int32_t *hop_log, double *time_out, int32_t *status_out, double *ws, double *flux_time)
 {
     extern __shared__ __align__(16) unsigned char sraw[];
     const int S = N + P;
@@ -84,6 +85,7 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
     uint8_t *occ = reinterpret_cast<uint8_t *>(red + 32);     // [S]
     __shared__ int ev_min;
     __shared__ double sh_total, sh_hop_time;
+    __shared__ double sh_flux[64];   // expected net inflow of each electrode (flux_time only)
 
     double *invd = ws;                  // [N*N] 1/d_ij
     double *ird = ws + (size_t)N * N;   // [N*N] (I_0 R)/d_ij
@@ -141,6 +143,18 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
         }
         double blocktot;
         const double base = block_exclusive_scan(lsum, red, blocktot);
+        if (flux_time) {
+            // every rate of this state is in cum (the scan synchronised): the
+            // expected net hole flow into each electrode, column N+e minus
+            // row N+e, summed in ascending site order
+            for (int e = tid; e < P; e += kThreads) {
+                double in = 0.0, out = 0.0;
+                for (int i = 0; i < N; ++i) in += cum[(size_t)i * S + N + e];
+                for (int j = 0; j < N; ++j) out += cum[(size_t)(N + e) * S + j];
+                sh_flux[e] = in - out;
+            }
+            __syncthreads();
+        }
         // running sums continued from the chunk's base
         double run = base;
         for (int k = kb; k < ke; ++k) {
@@ -186,6 +200,8 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
             if (to < N) occ[to] = 1; else eo[to - N] += 1;
             if (record) traffic[(size_t)from * S + to] += 1.0;
             if (hop_log) { hop_log[2 * hop] = from; hop_log[2 * hop + 1] = to; }
+            if (flux_time)
+                for (int e = 0; e < P; ++e) flux_time[e] += sh_flux[e] * hop_time;
             sh_hop_time = hop_time;
         }
         __syncthreads();
@@ -202,6 +218,42 @@ __global__ void __launch_bounds__(kThreads) f64_chain_kernel(
     }
 }
 
+__global__ void __launch_bounds__(kThreads) f64_chain_kernel(
+    int N, int P, double nu, double kT, double I0, double R, uint8_t *occ_g, const double *d,
+    const double *Ec, const double *se_in, const double *tc, int64_t *eo, int64_t hops,
+    int record, double *traffic, double *oit, const double *uniforms, uint64_t seed,
+    int32_t *hop_log, double *time_out, int32_t *status_out, double *ws, double *flux_time)
+{
+    f64_chain(N, P, nu, kT, I0, R, occ_g, d, Ec, se_in, tc, eo, hops, record, traffic, oit, uniforms,
+              seed, hop_log, time_out, status_out, ws, flux_time);
+}
+
+// Many independent chains in one launch, one block each (Philox streams
+// keyed by each chain's own seed).
+__global__ void __launch_bounds__(kThreads) f64_batch_kernel(const kmc_f64_batch B, size_t ws_doubles)
+{
+    const int c = blockIdx.x;
+    const int N = B.N[c], P = B.P[c];
+    // a chain whose sizes do not fit the launch (shared memory is sized for
+    // max_sites, the flux buffer for 64 electrodes) stops before any access
+    if (N < 0 || P < 0 || N + P <= 0 || N + P > B.max_sites || (B.flux_time && P > 64) || !(B.kT[c] > 0.0) ||
+        B.hops[c] < 0) {
+        if (threadIdx.x == 0) {
+            B.status_out[c] = KMC_ERR_INVALID;
+            B.time_out[c] = 0.0;
+        }
+        return;
+    }
+    const int64_t so = B.site_off[c], eo = B.el_off[c], po = B.pair_off[c], vo = B.se_off[c];
+    double *fx = B.flux_time ? B.flux_time + eo : nullptr;
+    double *tr = B.record ? B.traffic + B.traffic_off[c] : nullptr;
+    double *oit = B.record ? B.occupations_in_time + so : nullptr;
+    f64_chain(N, P, B.nu[c], B.kT[c], B.I_0[c], B.R[c], B.occupation + so, B.distances + po, B.E_constant + so,
+              B.site_energies + vo, B.transitions_constant + po, B.electrode_occupation + eo, B.hops[c],
+              B.record, tr, oit, nullptr, B.seeds[c], nullptr, B.time_out + c, B.status_out + c,
+              B.workspace + (size_t)c * ws_doubles, fx);
+}
+
 }  // namespace
 
 size_t f64_workspace_size(int S)
@@ -213,7 +265,7 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
                  const double *d, const double *Ec, const double *se, const double *tc,
                  int64_t *eo, int64_t hops, int record, double *traffic, double *oit,
                  const double *uniforms, uint64_t seed, int32_t *hop_log, double *time_out,
-                 int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st)
+                 int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st, double *flux_time)
 {
     const int S = N + P;
     if (N < 0 || P < 0 || S <= 0 || S > kMaxSitesF64 || hops < 0)
@@ -226,6 +278,7 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
     if (ws_bytes < f64_workspace_size(S))
         return fail(KMC_ERR_INVALID, "simulate_f64: workspace %zu bytes < %zu", ws_bytes, f64_workspace_size(S));
     if (!(kT > 0)) return fail(KMC_ERR_INVALID, "simulate_f64: kT must be positive");
+    if (flux_time && P > 64) return fail(KMC_ERR_INVALID, "simulate_f64: flux_time supports at most 64 electrodes");
     const size_t smem = sizeof(double) * (S + 32) + S + 16;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(f64_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -234,12 +287,46 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
     }
     f64_chain_kernel<<<1, kThreads, smem, st>>>(N, P, nu, kT, I0, R, occ, d, Ec, se, tc, eo, hops,
                                                 record, traffic, oit, uniforms, seed, hop_log,
-                                                time_out, status_out, static_cast<double *>(ws));
+                                                time_out, status_out, static_cast<double *>(ws), flux_time);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "f64 launch");
     return KMC_OK;
 }
 
+
+size_t f64_batch_workspace_size(int n_chains, int max_sites)
+{
+    return (size_t)n_chains * f64_workspace_size(max_sites);
+}
+
+int simulate_f64_batch(const kmc_f64_batch &B, cudaStream_t st)
+{
+    if (B.n_chains < 0 || B.max_sites <= 0 || B.max_sites > kMaxSitesF64)
+        return fail(KMC_ERR_INVALID, "simulate_f64_batch: bad sizes (n_chains %d, max_sites %d)", B.n_chains,
+                    B.max_sites);
+    if (B.n_chains == 0) return KMC_OK;
+    if (!B.N || !B.P || !B.nu || !B.kT || !B.I_0 || !B.R || !B.pair_off || !B.distances ||
+        !B.transitions_constant || !B.site_off || !B.E_constant || !B.se_off || !B.site_energies ||
+        !B.occupation || !B.el_off || !B.electrode_occupation || !B.hops || !B.seeds || !B.time_out ||
+        !B.status_out || !B.workspace)
+        return fail(KMC_ERR_INVALID, "simulate_f64_batch: a required pointer is NULL");
+    if (B.record && (!B.traffic || !B.traffic_off || !B.occupations_in_time))
+        return fail(KMC_ERR_INVALID, "simulate_f64_batch: record needs traffic, traffic_off, occupations_in_time");
+    if (B.workspace_bytes < f64_batch_workspace_size(B.n_chains, B.max_sites))
+        return fail(KMC_ERR_INVALID, "simulate_f64_batch: workspace %zu bytes < %zu", B.workspace_bytes,
+                    f64_batch_workspace_size(B.n_chains, B.max_sites));
+    // per-chain sizes are checked by each block (KMC_ERR_INVALID in status_out)
+    const int S = B.max_sites;
+    const size_t smem = sizeof(double) * (S + 32) + S + 16;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(f64_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute(f64 batch)");
+    }
+    f64_batch_kernel<<<B.n_chains, kThreads, smem, st>>>(B, f64_workspace_size(S) / sizeof(double));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "f64 batch launch");
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant
@@ -301,5 +388,5 @@ extern "C" int kmc_simulate_f64_static(int32_t n_acceptors, int32_t n_electrodes
                         site_energies, transitions_constant, electrode_occupation, hops, record,
                         traffic, occupations_in_time, uniforms, seed, hop_log, time_out, status_out,
                         ws, sizeof(double) * 3 * (size_t)kStaticWorkspaceSites * kStaticWorkspaceSites,
-                        static_cast<cudaStream_t>(stream));
+                        static_cast<cudaStream_t>(stream), nullptr);
 }

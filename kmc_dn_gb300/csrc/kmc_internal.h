@@ -30,8 +30,11 @@ int simulate_f64(int N, int P, double nu, double kT, double I0, double R, uint8_
                  const double *d, const double *Ec, const double *se, const double *tc,
                  int64_t *eo, int64_t hops, int record, double *traffic, double *oit,
                  const double *uniforms, uint64_t seed, int32_t *hop_log, double *time_out,
-                 int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st);
+                 int32_t *status_out, void *ws, size_t ws_bytes, cudaStream_t st,
+                 double *flux_time = nullptr);
 size_t f64_workspace_size(int S);
+size_t f64_batch_workspace_size(int n_chains, int max_sites);
+int simulate_f64_batch(const kmc_f64_batch &b, cudaStream_t st);
 
 // Host-buffer batch run (FP64 host inputs, copies in/out, synchronous).
 struct HostRun {

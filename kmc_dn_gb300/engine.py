@@ -56,12 +56,13 @@ def _dev(a, dtype, dev):
 
 def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_energies,
                  transitions_constant, hops, *, electrode_occupation=None, record=False,
-                 uniforms=None, seed=0, hop_log=False, dev=None, stream=None):
+                 uniforms=None, seed=0, hop_log=False, dev=None, stream=None, flux=False):
     """Run one chain on the plain FP64 kernel.
 
     Returns dict(time, occupation, electrode_occupation, traffic,
-    occupations_in_time, hop_log, status).  ``uniforms`` (2*hops values in
-    (0,1)) switches on replay mode."""
+    occupations_in_time, hop_log, status[, flux_time]).  ``uniforms``
+    (2*hops values in (0,1)) switches on replay mode; ``flux`` adds the time
+    integral of each electrode's expected net inflow."""
     d = device(dev)
     S = N + P
     hops = int(hops)
@@ -86,10 +87,15 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     L = lib()
     wsb = L.kmc_simulate_f64_workspace_size(S)
     ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
-    check(L.kmc_simulate_f64(N, P, float(nu), float(kT), float(I_0), float(R), _ptr(occ), _ptr(dist),
-                             _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), hops, int(bool(record)),
-                             _ptr(traffic), _ptr(oit), _ptr(u), int(seed) & (2**64 - 1), _ptr(log),
-                             _ptr(t_out), _ptr(st_out), _ptr(ws), wsb, _stream_handle(stream)))
+    fx = torch.zeros(max(P, 1), dtype=f64, device=d) if flux else None
+    args = (N, P, float(nu), float(kT), float(I_0), float(R), _ptr(occ), _ptr(dist),
+            _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), hops, int(bool(record)),
+            _ptr(traffic), _ptr(oit), _ptr(u), int(seed) & (2**64 - 1), _ptr(log),
+            _ptr(t_out), _ptr(st_out), _ptr(ws), wsb, _stream_handle(stream))
+    if flux:
+        check(L.kmc_simulate_f64_flux(*args, _ptr(fx)))
+    else:
+        check(L.kmc_simulate_f64(*args))
     torch.cuda.synchronize(d)
     out = dict(time=float(t_out.item()), occupation=occ.cpu().numpy().astype(bool),
                electrode_occupation=eo.cpu().numpy(), status=int(st_out.item()))
@@ -97,6 +103,8 @@ def simulate_f64(N, P, nu, kT, I_0, R, occupation, distances, E_constant, site_e
     out["occupations_in_time"] = oit.cpu().numpy()[:N] if record else np.zeros(N)
     if hop_log:
         out["hop_log"] = log.cpu().numpy()[: 2 * hops].reshape(hops, 2)
+    if flux:
+        out["flux_time"] = fx.cpu().numpy()[:P]
     return out
 
 
@@ -135,50 +143,97 @@ class CancelWord:
             pass
 
 
-def simulate_f64_many(chains, hops, seeds, *, n_streams=32, dev=None, record=False):
-    """Run independent FP64 chains concurrently (one kernel launch per chain,
-    spread over ``n_streams`` CUDA streams), for FP64 reference statistics.
+def simulate_f64_many(chains, hops, seeds, *, dev=None, record=False, flux=False, n_streams=None):
+    """Run independent FP64 chains of the plain FP64 kernel in one launch
+    (kmc_simulate_f64_batch: one block per chain), for FP64 reference
+    statistics.
 
     ``chains``: list of dicts with N, P, nu, kT, I_0, R, occupation,
-    distances, E_constant, site_energies, transitions_constant.  Returns
+    distances, E_constant, site_energies, transitions_constant (chains
+    whose distances / transitions_constant are the same arrays share one
+    device copy).  ``hops``: one budget or one per chain.  Returns
     (time[C], electrode_occupation[C][P], status[C]) and, with ``record``,
-    a fourth list: occupations_in_time[C][N] (numba convention)."""
+    a fourth list: occupations_in_time[C][N] (numba convention); with
+    ``flux`` a last list: the time integral of each electrode's expected net
+    inflow.  (``n_streams`` is accepted for compatibility and unused.)"""
     d = device(dev)
-    f64 = torch.float64
+    f64, i64 = torch.float64, torch.int64
+    n = len(chains)
+    if n == 0:
+        return (np.zeros(0), [], np.zeros(0, np.int32)) + (([],) if record else ()) + (([],) if flux else ())
+    Ns = np.array([int(ch["N"]) for ch in chains], np.int32)
+    Ps = np.array([int(ch["P"]) for ch in chains], np.int32)
+    Ss = Ns + Ps
+    # shared pair tables: one device block per distinct (distances, tc) pair of arrays
+    blocks, key_of, pair_off = [], {}, np.zeros(n, np.int64)
+    off = 0
+    for c, ch in enumerate(chains):
+        k = (id(ch["distances"]), id(ch["transitions_constant"]))
+        if k not in key_of:
+            key_of[k] = off
+            blocks.append((np.asarray(ch["distances"], np.float64).reshape(-1),
+                           np.asarray(ch["transitions_constant"], np.float64).reshape(-1)))
+            off += int(Ss[c]) ** 2
+        pair_off[c] = key_of[k]
+    cat = lambda xs, dt: np.ascontiguousarray(np.concatenate([np.asarray(x, dt).reshape(-1) for x in xs]))  # noqa: E731
+    site_off = np.concatenate([[0], np.cumsum(Ns)[:-1]]).astype(np.int64)
+    se_off = np.concatenate([[0], np.cumsum(Ss)[:-1]]).astype(np.int64)
+    el_off = np.concatenate([[0], np.cumsum(Ps)[:-1]]).astype(np.int64)
+    tr_off = np.concatenate([[0], np.cumsum(Ss.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+    smax = int(Ss.max())
+    T = lambda a, dt: _dev(a, dt, d)  # noqa: E731
+    keep = dict(
+        N=T(Ns, torch.int32), P=T(Ps, torch.int32),
+        nu=T([float(ch["nu"]) for ch in chains], f64), kT=T([float(ch["kT"]) for ch in chains], f64),
+        I_0=T([float(ch["I_0"]) for ch in chains], f64), R=T([float(ch["R"]) for ch in chains], f64),
+        pair_off=T(pair_off, i64), distances=T(cat([b[0] for b in blocks], np.float64), f64),
+        tc=T(cat([b[1] for b in blocks], np.float64), f64),
+        site_off=T(site_off, i64), Ec=T(cat([ch["E_constant"] for ch in chains], np.float64), f64),
+        se_off=T(se_off, i64), se=T(cat([ch["site_energies"] for ch in chains], np.float64), f64),
+        occ=T(cat([ch["occupation"] for ch in chains], np.uint8), torch.uint8),
+        el_off=T(el_off, i64), eo=torch.zeros(max(int(Ps.sum()), 1), dtype=i64, device=d),
+        hops=T(np.broadcast_to(np.asarray(hops, np.int64), (n,)), i64),
+        seeds=T(np.asarray([int(s_) & (2**64 - 1) for s_ in seeds], np.uint64).view(np.int64), i64),
+        t_out=torch.zeros(n, dtype=f64, device=d), s_out=torch.zeros(n, dtype=torch.int32, device=d))
     L = lib()
-    streams = [torch.cuda.Stream(d) for _ in range(max(1, min(n_streams, len(chains))))]
-    keep, outs = [], []
-    torch.cuda.synchronize(d)
-    for k, (ch, seed) in enumerate(zip(chains, seeds)):
-        N, P = int(ch["N"]), int(ch["P"])
-        S = N + P
-        st = streams[k % len(streams)]
-        with torch.cuda.stream(st):
-            occ = _dev(np.asarray(ch["occupation"], np.uint8).reshape(N), torch.uint8, d)
-            dist = _dev(np.asarray(ch["distances"], np.float64).reshape(S, S), f64, d)
-            tc = _dev(np.asarray(ch["transitions_constant"], np.float64).reshape(S, S), f64, d)
-            ec = _dev(np.asarray(ch["E_constant"], np.float64).reshape(N), f64, d)
-            se = _dev(np.asarray(ch["site_energies"], np.float64).reshape(S), f64, d)
-            eo = torch.zeros(max(P, 1), dtype=torch.int64, device=d)
-            t_out = torch.zeros(1, dtype=f64, device=d)
-            s_out = torch.zeros(1, dtype=torch.int32, device=d)
-            tr = torch.zeros(S * S, dtype=f64, device=d) if record else None
-            oit = torch.zeros(max(N, 1), dtype=f64, device=d) if record else None
-            wsb = L.kmc_simulate_f64_workspace_size(S)
-            ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
-        check(L.kmc_simulate_f64(N, P, float(ch["nu"]), float(ch["kT"]), float(ch["I_0"]), float(ch["R"]),
-                                 _ptr(occ), _ptr(dist), _ptr(ec), _ptr(se), _ptr(tc), _ptr(eo), int(hops),
-                                 int(bool(record)), _ptr(tr), _ptr(oit), None, int(seed) & (2**64 - 1), None,
-                                 _ptr(t_out), _ptr(s_out), _ptr(ws), wsb, _stream_handle(st)))
-        keep.append((occ, dist, tc, ec, se, ws, tr))
-        outs.append((t_out, eo, s_out, P, oit, N))
-    torch.cuda.synchronize(d)
-    times = np.array([float(o[0].item()) for o in outs])
-    eos = [o[1].cpu().numpy()[:o[3]] for o in outs]
-    status = np.array([int(o[2].item()) for o in outs])
+    wsb = L.kmc_simulate_f64_batch_workspace_size(n, smax)
+    keep["ws"] = torch.empty(max(wsb, 8), dtype=torch.uint8, device=d)
+    b = _native.KmcF64Batch()
+    b.n_chains, b.max_sites, b.record = n, smax, int(bool(record))
+    b.N, b.P = keep["N"].data_ptr(), keep["P"].data_ptr()
+    b.nu, b.kT, b.I_0, b.R = (keep[k].data_ptr() for k in ("nu", "kT", "I_0", "R"))
+    b.pair_off, b.distances, b.transitions_constant = (keep["pair_off"].data_ptr(), keep["distances"].data_ptr(),
+                                                       keep["tc"].data_ptr())
+    b.site_off, b.E_constant = keep["site_off"].data_ptr(), keep["Ec"].data_ptr()
+    b.se_off, b.site_energies = keep["se_off"].data_ptr(), keep["se"].data_ptr()
+    b.occupation, b.el_off, b.electrode_occupation = (keep["occ"].data_ptr(), keep["el_off"].data_ptr(),
+                                                      keep["eo"].data_ptr())
+    b.hops, b.seeds = keep["hops"].data_ptr(), keep["seeds"].data_ptr()
     if record:
-        return times, eos, status, [o[4].cpu().numpy()[:o[5]] for o in outs]
-    return times, eos, status
+        keep["tr_off"] = T(tr_off, i64)
+        keep["tr"] = torch.zeros(max(int((Ss.astype(np.int64) ** 2).sum()), 1), dtype=f64, device=d)
+        keep["oit"] = torch.zeros(max(int(Ns.sum()), 1), dtype=f64, device=d)
+        b.traffic_off, b.traffic, b.occupations_in_time = (keep["tr_off"].data_ptr(), keep["tr"].data_ptr(),
+                                                           keep["oit"].data_ptr())
+    if flux:
+        keep["fx"] = torch.zeros(max(int(Ps.sum()), 1), dtype=f64, device=d)
+        b.flux_time = keep["fx"].data_ptr()
+    b.time_out, b.status_out = keep["t_out"].data_ptr(), keep["s_out"].data_ptr()
+    b.workspace, b.workspace_bytes = keep["ws"].data_ptr(), wsb
+    check(L.kmc_simulate_f64_batch(C.byref(b), _stream_handle()))
+    torch.cuda.synchronize(d)
+    times = keep["t_out"].cpu().numpy()
+    eo = keep["eo"].cpu().numpy()
+    eos = [eo[o:o + p] for o, p in zip(el_off, Ps)]
+    status = keep["s_out"].cpu().numpy()
+    res = [times, eos, status]
+    if record:
+        oit = keep["oit"].cpu().numpy()
+        res.append([oit[o:o + k] for o, k in zip(site_off, Ns)])
+    if flux:
+        fx = keep["fx"].cpu().numpy()
+        res.append([fx[o:o + p] for o, p in zip(el_off, Ps)])
+    return tuple(res)
 
 
 # ---------------------------------------------------------------------------
@@ -353,7 +408,7 @@ class Batch:
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
                  pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False,
-                 measure_drift=False, persistent=False):
+                 measure_drift=False, persistent=False, flux=False):
         self.dev = device(dev)
         d = self.dev
         tables_set = tables if isinstance(tables, TableSet) else None
@@ -444,6 +499,8 @@ class Batch:
         # debug builds: per chain, hops an FP64 selection would pick differently
         self.select_mismatch = (torch.zeros(n, dtype=torch.int64, device=d)
                                 if count_select_mismatch else None)
+        # electrode pool: time integral of each electrode's expected net inflow
+        self.flux_time = torch.zeros(max(nel, 1), dtype=torch.float64, device=d) if flux else None
         # per chain: largest incremental-energy drift found at a re-anchor (kT)
         self.energy_drift = torch.zeros(n, dtype=torch.float32, device=d) if measure_drift else None
         self.cancel = None            # a CancelWord, or None
@@ -512,6 +569,8 @@ class Batch:
             b.select_mismatch = self.select_mismatch.data_ptr()
         if self.energy_drift is not None:
             b.energy_drift = self.energy_drift.data_ptr()
+        if self.flux_time is not None:
+            b.flux_time = self.flux_time.data_ptr()
         if self.hop_log is not None:
             b.hop_log, b.hop_log_off = self.hop_log.data_ptr(), self.hop_log_off.data_ptr()
             if self.hop_rates is not None:
@@ -570,6 +629,9 @@ class Batch:
             out["select_mismatch"] = self.select_mismatch.cpu().numpy()
         if self.energy_drift is not None:
             out["energy_drift"] = self.energy_drift.cpu().numpy()
+        if self.flux_time is not None:
+            ft = self.flux_time.cpu().numpy()
+            out["flux_time"] = [ft[o:o + p] for o, p in zip(self.el_off, self.P_c)]
         if self.hop_log is not None:
             ht = self.hops_total.cpu().numpy()
             lg = self.hop_log.cpu().numpy()

@@ -431,6 +431,37 @@ def test_persistent_launch_gives_the_static_launch_results(engine_lib, pair_mode
     for r in (p, q):
         np.testing.assert_array_equal(a["time"], r["time"])
         np.testing.assert_array_equal(a["hops_done"], r["hops_done"])
-        for k in ("electrode_occupation", "occupation", "traffic", "occ_time"):
+        for k in ("electrode_occupation", "occupation", "traffic"):
             for x, y in zip(a[k], r[k]):
                 np.testing.assert_array_equal(x, y)
+    for x, y in zip(a["occ_time"], p["occ_time"]):
+        np.testing.assert_array_equal(x, y)
+    # a split run closes each occupied site's interval at every launch end and
+    # adds the pieces: the same sum in another order, equal to rounding
+    for x, y in zip(a["occ_time"], q["occ_time"]):
+        np.testing.assert_allclose(x, y, rtol=1e-14, atol=0)
+
+
+def test_f64_batch_launch_equals_single_chain_runs(engine_lib):
+    """kmc_simulate_f64_batch (one block per chain, one launch) runs each
+    chain exactly as kmc_simulate_f64 does with the same seed: times,
+    electrode counts, final states, recorded occupancy times and flux
+    integrals bit for bit, for networks of different sizes in one launch."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import simulate_f64, simulate_f64_many
+    nets = [n for n, _ in workloads.uneven_batch(6, seed=8, hops_range=(1000, 1000))]
+    nets.append(workloads.plain_network(1))
+    chains = [dict(N=n.N, P=n.P, nu=n.nu, kT=n.kT, I_0=n.I_0, R=n.R, occupation=n.occupation.astype(np.uint8),
+                   distances=n.distances, E_constant=n.E_constant(), site_energies=n.site_energies(),
+                   transitions_constant=n.transitions_constant) for n in nets]
+    seeds = [101 + 7 * k for k in range(len(nets))]
+    hops = 1500
+    t, eo, st, oit, fx = simulate_f64_many(chains, hops, seeds, record=True, flux=True)
+    np.testing.assert_array_equal(st, 0)
+    for k, (n, ch) in enumerate(zip(nets, chains)):
+        r = simulate_f64(n.N, n.P, n.nu, n.kT, n.I_0, n.R, ch["occupation"], n.distances, ch["E_constant"],
+                         ch["site_energies"], n.transitions_constant, hops, record=True, seed=seeds[k], flux=True)
+        assert r["time"] == t[k]
+        np.testing.assert_array_equal(r["electrode_occupation"], eo[k])
+        np.testing.assert_array_equal(r["occupations_in_time"], oit[k])
+        np.testing.assert_array_equal(r["flux_time"], fx[k])
