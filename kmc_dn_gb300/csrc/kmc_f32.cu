@@ -137,6 +137,16 @@ __device__ __forceinline__ F2 two_sum(float a, float b)
     return F2{s, e};
 }
 
+// hi + lo += c: the rounding error of the high-part add (TwoSum) goes to the
+// low part, so a long series of increments keeps its exact sum to ~2^-47
+// instead of accumulating one rounding per increment.
+__device__ __forceinline__ void comp_add(float &hi, float &lo, float c)
+{
+    const F2 s = two_sum(hi, c);
+    hi = s.hi;
+    lo = __fadd_rn(lo, s.lo);
+}
+
 // (x + y), normalised so that |lo| <= ulp(hi) / 2
 __device__ __forceinline__ F2 df_add(F2 x, F2 y)
 {
@@ -625,7 +635,8 @@ struct ChainSmem {
     Rec *tgt;        // [S+1] target records
     int *src_id;     // [S+1] site ids of the sources
     int *tgt_id;     // [S+1] site ids of the targets
-    float *E;        // [S]   site energies (acceptors)
+    float *E;        // [S]   site energies (acceptors), high part
+    float *Elo;      // [S]   their low parts: E + Elo carries the energy to ~2^-47
     uint32_t *occw;  // [W]   occupancy bits
     int *eo;         // [kMaxElectrodes] electrode counters of this launch
     float *rates;    // [rate_words] this hop's pair rates, or nullptr (recompute)
@@ -639,7 +650,7 @@ __host__ __device__ __forceinline__ int chain_list_words(int S)
 {
     const int W = (S + 31) / 32;
     const int rw = static_cast<int>(sizeof(Rec) / 4);
-    const int words = 2 * rw * (S + 1) + 2 * (S + 1) + S + W + kMaxElectrodes;
+    const int words = 2 * rw * (S + 1) + 2 * (S + 1) + 2 * S + W + kMaxElectrodes;
     return (words + 3) & ~3;
 }
 
@@ -661,7 +672,8 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_
     c.src_id = reinterpret_cast<int *>(c.tgt + (S + 1));
     c.tgt_id = c.src_id + (S + 1);
     c.E = reinterpret_cast<float *>(c.tgt_id + (S + 1));
-    c.occw = reinterpret_cast<uint32_t *>(c.E + S);
+    c.Elo = c.E + S;
+    c.occw = reinterpret_cast<uint32_t *>(c.Elo + S);
     c.eo = reinterpret_cast<int *>(c.occw + (S + 31) / 32);
     c.rates = rate_words > 0 ? reinterpret_cast<float *>(base + chain_list_words<Rec>(S)) : nullptr;
 #ifdef KMC_DEBUG_CHECKS
@@ -750,12 +762,13 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     Rec el_rec{};
     auto anchor_and_build = [&](bool drift) {
         for (int j = g; j < N; j += G) {
-            float acc = 0.0f;
+            // E_j = Ec_j - sum_{k empty} B_jk, summed with compensation
+            float hi = Ec[j], lo = 0.0f;
             for (int k = 0; k < N; ++k)
-                if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) acc += pairs.coulomb(j, k);
-            const float e = Ec[j] - acc;
-            if (drift) drift_max = fmaxf(drift_max, fabsf(e - sm.E[j]));
-            sm.E[j] = e;
+                if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) comp_add(hi, lo, -pairs.coulomb(j, k));
+            if (drift) drift_max = fmaxf(drift_max, fabsf((hi - sm.E[j]) + (lo - sm.Elo[j])));
+            sm.E[j] = hi;
+            sm.Elo[j] = lo;
         }
         const int z = N - h;
         int wcur = 0, cum = 0;
@@ -764,7 +777,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
             const uint32_t word = sm.occw[w];
             const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
-            const Rec r = pairs.rec(j, cs * sm.E[j]);
+            const Rec r = pairs.rec(j, cs * (sm.E[j] + sm.Elo[j]));
             if ((word >> (j & 31)) & 1u) {
                 sm.src[below] = r;
                 if (!Pairs::kSiteInRec) sm.src_id[below] = j;
@@ -1088,10 +1101,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         {
             int wcur = 0, cum = 0;
             for (int j = g; j < N; j += G) {
-                float Ej = sm.E[j];
-                if (fa && j != from) Ej -= pairs.coulomb(j, from);
-                if (tb && j != to) Ej += pairs.coulomb(j, to);
+                // O(N) update (makeJump, simulation.go:107-130), compensated
+                float Ej = sm.E[j], Elo = sm.Elo[j];
+                if (fa && j != from) comp_add(Ej, Elo, -pairs.coulomb(j, from));
+                if (tb && j != to) comp_add(Ej, Elo, pairs.coulomb(j, to));
                 sm.E[j] = Ej;
+                sm.Elo[j] = Elo;
                 const int w = j >> 5;
                 while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
                 const uint32_t word = sm.occw[w];
@@ -1105,7 +1120,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     continue;
                 }
 #endif
-                const Rec r = pairs.rec(j, cs * Ej);
+                const Rec r = pairs.rec(j, cs * (Ej + Elo));
                 if (occ_j) {
                     sm.src[below] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[below] = j;
