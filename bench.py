@@ -134,7 +134,27 @@ def cpu_baseline(net, V, threads, hops, n_chains, budget_s=20.0):
 FLOOR = 0.05     # currents judged at the 1 % level: |I| >= 5 % of the voltage vector's largest |I|
 
 
-def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0, pair_mode="table"):
+def _current_stats(I32, I64):
+    """Per current: difference of the means, its standard error, z-score,
+    relative difference and 3-sigma relative upper bound."""
+    m32, m64 = I32.mean(0), I64.mean(0)
+    se = np.sqrt(I32.var(0, ddof=1) / len(I32) + I64.var(0, ddof=1) / len(I64))
+    d = np.abs(m32 - m64)
+    den = np.maximum(np.abs(m64), 1e-300)
+    return m64, se, d / np.maximum(se, 1e-300), d / den, (d + 3.0 * se) / den
+
+
+def _summary(z, rel, up, ab):
+    return {"max_abs_z": float(z.max()), "frac_within_3sigma": float(np.mean(z <= 3.0)),
+            "resolved_within_1pct_at_3sigma": int(np.sum(ab & (up <= 0.01))),
+            "point_estimate_within_1pct": int(np.sum(ab & (rel <= 0.01))),
+            "max_rel_diff_above_floor": float(rel[ab].max()),
+            "median_rel_diff_above_floor": float(np.median(rel[ab])),
+            "max_rel_upper3_above_floor": float(up[ab].max()),
+            "median_rel_upper3_above_floor": float(np.median(up[ab]))}
+
+
+def accuracy_of(cases, dev, replicas32=512, replicas64=128, hops=300_000, seed=0, pair_mode="table"):
     """Electrode currents and occupations of the FP32 engine against the
     plain FP64 kernel (whose hop sequences equal the reference loop's, bit
     for bit), on independent replicas of each case.
@@ -142,13 +162,22 @@ def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0,
     ``cases``: (network, voltages) pairs.  The FP32 chains take their
     constant site energies from the device superposition (kmc_site_energies,
     the path the timed workloads use); the FP64 chains take the host's FP64
-    E_constant (the reference's set-up arithmetic).  Per current: the
-    z-score of the difference of the means and, for every current above the
-    magnitude floor (FLOOR of the vector's largest current), the relative
-    difference and its 3-sigma upper bound (|dI| + 3 SE) / |I_FP64|; such a
-    current is resolved at the 1 % level when that bound is <= 1 %.  Per
-    site the time-averaged occupation likewise (z-score and absolute
-    difference; both kernels credit occupancy after the hop)."""
+    E_constant (the reference's set-up arithmetic).
+
+    Two estimates of each current per chain: the count one, electrode
+    hops / time (what the reference reports), and a control-variate one,
+    count - beta * (count - flux) / time, where flux is the time integral of
+    the electrode's expected net inflow (flux_time): count - flux is a
+    zero-mean martingale, so any beta keeps the estimate unbiased, and beta
+    (fitted per current on both sides' pooled within-side deviations, the
+    same beta for both) removes the hop-by-hop Poisson noise the count
+    carries.  Per current: the z-score of the difference of the means and,
+    for every current above the magnitude floor (FLOOR of the vector's
+    largest current), the relative difference and its 3-sigma upper bound
+    (|dI| + 3 SE) / |I_FP64|; such a current is resolved at the 1 % level
+    when that bound is <= 1 %.  Per site the time-averaged occupation
+    likewise (z-score and absolute difference; both kernels credit
+    occupancy after the hop)."""
     import torch
     from kmc_dn_gb300 import _native
     from kmc_dn_gb300.engine import Batch, TableSpec, simulate_f64_many, superpose
@@ -164,7 +193,8 @@ def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0,
     b = Batch(specs, np.array(rows, np.int32), [cases[c][0].kT for c in rows], None, None,
               [cases[c][0].occupation.astype(np.uint8) for c in rows], np.full(len(rows), hops),
               streams=np.arange(len(rows)) + 10_000_000, seed=seed + 101, dev=dev, pair_mode=pair_mode,
-              record=_native.RECORD_NUMBA, E_constant_dev=torch.cat(ec_parts), el_energy_dev=torch.cat(ve_parts))
+              record=_native.RECORD_NUMBA, E_constant_dev=torch.cat(ec_parts), el_energy_dev=torch.cat(ve_parts),
+              flux=True)
     t0 = time.perf_counter()
     r32 = b.run().results()
     t32 = time.perf_counter() - t0
@@ -174,22 +204,30 @@ def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0,
                    distances=n.distances, E_constant=n.E_constant(v), site_energies=n.site_energies(v),
                    transitions_constant=n.transitions_constant) for n, v in (cases[c] for c in rows64)]
     t0 = time.perf_counter()
-    t64, eo64, st64, oit64 = simulate_f64_many(chains, hops, [seed * 7919 + 13 + i for i in range(len(rows64))],
-                                               dev=dev, n_streams=128, record=True)
+    t64, eo64, st64, oit64, fx64 = simulate_f64_many(
+        chains, hops, [seed * 7919 + 13 + i for i in range(len(rows64))], dev=dev, record=True, flux=True)
     tf64 = time.perf_counter() - t0
     assert np.all(st64 == 0)
-    zs, rels, ups, above, ozs, odiff = [], [], [], [], [], []
+    cnt, cv, above, betas, vr, ozs, odiff = {"z": [], "rel": [], "up": []}, {"z": [], "rel": [], "up": []}, [], [], [], [], []
     for c in range(len(cases)):
         i32 = [i for i, rc in enumerate(rows) if rc == c]
         i64 = [i for i, rc in enumerate(rows64) if rc == c]
-        I32 = np.stack([r32["electrode_occupation"][i] / r32["time"][i] for i in i32])
-        I64 = np.stack([eo64[i] / t64[i] for i in i64])
-        m32, m64 = I32.mean(0), I64.mean(0)
-        se = np.sqrt(I32.var(0, ddof=1) / len(i32) + I64.var(0, ddof=1) / len(i64))
-        d = np.abs(m32 - m64)
-        zs.append(d / np.maximum(se, 1e-300))
-        rels.append(d / np.maximum(np.abs(m64), 1e-300))
-        ups.append((d + 3.0 * se) / np.maximum(np.abs(m64), 1e-300))
+        T32 = np.array([r32["time"][i] for i in i32])[:, None]
+        T64 = np.array([t64[i] for i in i64])[:, None]
+        C32 = np.stack([r32["electrode_occupation"][i] for i in i32]) / T32
+        C64 = np.stack([eo64[i] for i in i64]) / T64
+        D32 = C32 - np.stack([r32["flux_time"][i] for i in i32]) / T32
+        D64 = C64 - np.stack([fx64[i] for i in i64]) / T64
+        # beta per current from the pooled within-side deviations
+        dc = np.concatenate([C32 - C32.mean(0), C64 - C64.mean(0)])
+        dd = np.concatenate([D32 - D32.mean(0), D64 - D64.mean(0)])
+        beta = (dc * dd).sum(0) / np.maximum((dd * dd).sum(0), 1e-300)
+        betas.append(beta)
+        m64, se_c, z, rel, up = _current_stats(C32, C64)
+        cnt["z"].append(z), cnt["rel"].append(rel), cnt["up"].append(up)
+        _, se_v, z, rel, up = _current_stats(C32 - beta * D32, C64 - beta * D64)
+        cv["z"].append(z), cv["rel"].append(rel), cv["up"].append(up)
+        vr.append((se_c / np.maximum(se_v, 1e-300)) ** 2)
         above.append(np.abs(m64) >= FLOOR * np.abs(m64).max())
         O32 = np.stack([r32["occ_time"][i] / r32["time"][i] for i in i32])
         O64 = np.stack([oit64[i] / t64[i] for i in i64])
@@ -197,19 +235,19 @@ def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0,
         od = np.abs(O32.mean(0) - O64.mean(0))
         ozs.append(od / np.maximum(osd, 1e-12))
         odiff.append(od)
-    z, rel, up, ab = map(np.concatenate, (zs, rels, ups, above))
+    ab = np.concatenate(above)
+    cat = {k: np.concatenate(v) for k, v in cnt.items()}
+    catv = {k: np.concatenate(v) for k, v in cv.items()}
     oz, od = np.concatenate(ozs), np.concatenate(odiff)
-    return {"voltage_vectors": len(cases), "currents": int(z.size), "replicas_fp32": replicas32,
+    return {"voltage_vectors": len(cases), "currents": int(ab.size), "replicas_fp32": replicas32,
             "replicas_fp64": replicas64, "hops": hops,
-            "max_abs_z": float(z.max()), "frac_within_3sigma": float(np.mean(z <= 3.0)),
             "floor": f"|I| >= {FLOOR:g} x the vector's largest |I| (FP64)",
             "currents_above_floor": int(ab.sum()),
-            "resolved_within_1pct_at_3sigma": int(np.sum(ab & (up <= 0.01))),
-            "point_estimate_within_1pct": int(np.sum(ab & (rel <= 0.01))),
-            "max_rel_diff_above_floor": float(rel[ab].max()),
-            "median_rel_diff_above_floor": float(np.median(rel[ab])),
-            "max_rel_upper3_above_floor": float(up[ab].max()),
-            "median_rel_upper3_above_floor": float(np.median(up[ab])),
+            "count_estimate": _summary(cat["z"], cat["rel"], cat["up"], ab),
+            "control_variate_estimate": dict(_summary(catv["z"], catv["rel"], catv["up"], ab),
+                                             median_variance_reduction=float(np.median(np.concatenate(vr))),
+                                             beta_range=[float(np.concatenate(betas).min()),
+                                                         float(np.concatenate(betas).max())]),
             "occupancies": int(oz.size), "occupancy_max_abs_z": float(oz.max()),
             "occupancy_frac_within_3sigma": float(np.mean(oz <= 3.0)),
             "occupancy_max_abs_diff": float(od.max()),
@@ -218,7 +256,7 @@ def accuracy_of(cases, dev, replicas32=256, replicas64=64, hops=300_000, seed=0,
             "fp64_s": tf64}
 
 
-def accuracy_sample(net, V, dev, n_vectors=16, replicas32=256, replicas64=64, hops=300_000, seed=0):
+def accuracy_sample(net, V, dev, n_vectors=16, replicas32=512, replicas64=128, hops=300_000, seed=0):
     """``accuracy_of`` on the first ``n_vectors`` voltage vectors of the
     homogeneous workload."""
     out = accuracy_of([(net, V[k]) for k in range(n_vectors)], dev, replicas32, replicas64, hops, seed)
@@ -291,7 +329,7 @@ def accuracy_large(dev, seed=0, n_drift=64, drift_hops=100_000, replay_hops=300,
               distances=onet.distances, E_constant=onet.E_constant(), site_energies=onet.site_energies(),
               transitions_constant=onet.transitions_constant)
     t64, eo64, st64, oit64 = simulate_f64_many([ch] * n_occ, occ_hops, [seed * 31 + 7 + i for i in range(n_occ)],
-                                               dev=dev, n_streams=n_occ, record=True)
+                                               dev=dev, record=True)
     assert np.all(st64 == 0)
     O32 = np.stack([r32["occ_time"][i] / r32["time"][i] for i in range(n_occ)])
     O64 = np.stack([oit64[i] / t64[i] for i in range(n_occ)])

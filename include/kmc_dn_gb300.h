@@ -310,6 +310,10 @@ typedef struct kmc_batch {
      * is a zero-mean martingale, so it is a low-variance companion estimate
      * of the current (accuracy checks).  NULL: not computed */
     double *flux_time;
+    /* persistent launches only: at most this many blocks (0: as many as
+     * stay resident), so that launches of several size bins running side by
+     * side can share the device in proportion to their work */
+    int32_t max_grid;
 } kmc_batch;
 
 /*

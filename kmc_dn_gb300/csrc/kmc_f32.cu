@@ -1350,7 +1350,8 @@ int launch_warp_kernel(const kmc_batch &b, cudaStream_t st, int grid, size_t sme
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_engine_kernel<G, Pairs, 3>,
                                                                       wpb * 32, smem);
         if (e != cudaSuccess) return fail_cuda(e, "engine occupancy");
-        const int pgrid = min(grid, max(1, per_sm) * sm_count());
+        int pgrid = min(grid, max(1, per_sm) * sm_count());
+        if (b.max_grid > 0) pgrid = min(pgrid, b.max_grid);
         warp_engine_kernel<G, Pairs, 3><<<pgrid, wpb * 32, smem, st>>>(b, rw, tw);
         e = cudaGetLastError();
         return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
@@ -1407,6 +1408,7 @@ int launch_block_kernel(const kmc_batch &b, cudaStream_t st, size_t smem, int rw
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, block_engine_kernel<T, Pairs>, T, smem);
         if (e != cudaSuccess) return fail_cuda(e, "engine occupancy");
         grid = min(grid, max(1, per_sm) * sm_count());
+        if (b.max_grid > 0) grid = min(grid, b.max_grid);
     }
     block_engine_kernel<T, Pairs><<<grid, T, smem, st>>>(b, rw, tw);
     cudaError_t e = cudaGetLastError();
