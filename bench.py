@@ -265,7 +265,7 @@ def accuracy_sample(net, V, dev, n_vectors=16, replicas32=512, replicas64=128, h
     return out
 
 
-def accuracy_large(dev, seed=0, n_drift=64, drift_hops=100_000, replay_hops=300, n_occ=152, occ_hops=10_000):
+def accuracy_large(dev, seed=0, n_drift=64, drift_hops=100_000, replay_hops=300, n_occ=96, occ_hops=6_000):
     """FP32 error on the large networks (N = 1000, M = 100, 8 electrodes):
 
     * drift: the largest difference (kT) between the energies the O(N)

@@ -508,23 +508,8 @@ class Batch:
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
         # persistent launches: one work counter per bin, zeroed before each launch
         self.persistent = bool(persistent)
-        work = np.array([float(np.sum(np.broadcast_to(np.asarray(hops, np.float64), (n,))[bn["chains"]]
-                                      * self.S_c[bn["chains"]].astype(np.float64) ** 2)) for bn in self._bins])
-        self._bin_share = work / max(work.sum(), 1.0)
         self._counters = (torch.zeros(max(len(self._bins), 1), dtype=torch.int32, device=d)
                           if self.persistent else None)
-
-    def _resident_blocks(self, bin_):
-        """Blocks of this bin's launch the device holds at once, roughly:
-        by threads (2048 per SM) and by shared memory (227 KB per SM)."""
-        props = torch.cuda.get_device_properties(self.dev)
-        G = bin_["G"]
-        threads = 32 * self._warps(G) if G <= 32 else G
-        S = bin_["max_sites"]
-        chains = (32 * self._warps(G) // G) if G <= 32 else 1
-        smem = chains * (4 * (S * S // 3) + 48 * (S + 1) + 64 * 4)
-        per_sm = max(1, min(props.max_threads_per_multi_processor // threads, (227 * 1024) // max(smem, 1)))
-        return per_sm * props.multi_processor_count
 
     def _warps(self, G):
         w = self.warps_per_block
@@ -614,10 +599,6 @@ class Batch:
                 with torch.cuda.stream(st if st is not None else torch.cuda.current_stream()):
                     ctr.zero_()
                 b.work_counter = ctr.data_ptr()
-                if bin_streams and len(self._bins) > 1:
-                    # bins side by side: each gets a share of the device's
-                    # blocks in proportion to its work (chains x hops x S^2)
-                    b.max_grid = max(1, int(round(self._bin_share[i] * self._resident_blocks(bin_))))
             check(L.kmc_run_batch(C.byref(b), _stream_handle(st)))
         return self
 
