@@ -246,6 +246,38 @@ __device__ __forceinline__ uint64_t u01_fixed_from_double(double u)
     return __double2ull_rz(u * 0x1.0p64);
 }
 
+// Exact n / T for 0 <= n < 2^22 from inv ~ 1/T (float reciprocal, one
+// correction step), as in decode_pair below.
+__device__ __forceinline__ int div_small(int n, int T, float inv)
+{
+    int q = __float2int_rz(__int2float_rn(n) * inv);
+    const int r = n - q * T;
+    if (r < 0) --q; else if (r >= T) ++q;
+    return q;
+}
+
+// Row-aligned runs: thread g of a group of G walks the rows [row_bound(g),
+// row_bound(g + 1)) of the pair enumeration (h source rows of T1 targets,
+// then P rows of T2), the boundary nearest to pair g*A/G.  Every thread then
+// starts each of its rows at column 0, so the threads of a group step
+// through the same target column together.
+__device__ __forceinline__ int row_bound(int g, int G, int A, int A1, int h, int P, int T1, int T2,
+                                         float inv1, float inv2)
+{
+    if (g <= 0) return 0;
+    if (g >= G) return h + P;
+    const int k = static_cast<int>((static_cast<long long>(g) * A) / G);
+    if (k < A1) return min(h, div_small(k + (T1 >> 1), T1, inv1));
+    if (T2 <= 0) return h + P;
+    return min(h + P, h + div_small(k - A1 + (T2 >> 1), T2, inv2));
+}
+
+// First pair of row r.
+__device__ __forceinline__ int row_start(int r, int h, int A1, int T1, int T2)
+{
+    return r <= h ? r * T1 : A1 + (r - h) * T2;
+}
+
 // k -> (row, col) within the pair enumeration.  Float-reciprocal quotient
 // with one correction step: with inv within 2^-22 (relative) of 1/T and
 // k < 2^22 the estimate is off by less than one, so the result is exact (the
@@ -640,6 +672,7 @@ struct ChainSmem {
     uint32_t *occw;  // [W]   occupancy bits
     int *eo;         // [kMaxElectrodes] electrode counters of this launch
     float *rates;    // [rate_words] this hop's pair rates, or nullptr (recompute)
+    int rate_words;  // words of `rates`
 #ifdef KMC_DEBUG_CHECKS
     int rate_cap;    // words of `rates`
 #endif
@@ -676,6 +709,7 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_
     c.occw = reinterpret_cast<uint32_t *>(c.Elo + S);
     c.eo = reinterpret_cast<int *>(c.occw + (S + 31) / 32);
     c.rates = rate_words > 0 ? reinterpret_cast<float *>(base + chain_list_words<Rec>(S)) : nullptr;
+    c.rate_words = rate_words > 0 ? rate_words : 0;
 #ifdef KMC_DEBUG_CHECKS
     c.rate_cap = rate_words;
 #endif
@@ -844,66 +878,113 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (A <= 0) { status = KMC_ERR_NONFINITE; break; }
         const float inv1 = T1 > 0 ? rcp_approx(static_cast<float>(T1)) : 0.0f;
         const float inv2 = T2 > 0 ? rcp_approx(static_cast<float>(T2)) : 0.0f;
-        // Run length per thread.  Block groups round it up to an odd number:
+        // Two ways to split the A pairs into G contiguous runs.  Balanced:
+        // thread g takes [g*M, g*M + M) whatever the rows, and keeps track of
+        // row changes pair by pair.  Row-aligned: thread g takes whole rows
+        // [row_bound(g), row_bound(g + 1)), the boundaries nearest to pair
+        // g*A/G, so every thread starts each row at column 0: the threads of a
+        // group read the same target record at the same time (one broadcast
+        // load) and need no per-pair row bookkeeping, at the price of runs up
+        // to one row longer than A/G.  Row-aligned runs pay off when a run
+        // spans at least 1.5 rows.
+#ifdef KMC_FORCE_BALANCED_RUNS
+        const bool aligned = false;   // measurement builds: the balanced split only
+#else
+        const bool aligned = A >= ((3 * G * T1) >> 1);
+#endif
+        // Balanced run length.  Block groups round it up to an odd number:
         // thread g's run starts M records after thread g-1's, and with long
-        // rows (few row changes inside a run) an odd stride puts the threads'
-        // 8- or 16-byte record loads in distinct banks, where an even M made
-        // them collide up to 8-fold (30 % faster on N=1000 networks).  Warp
-        // slices walk short rows whose wrap scrambles the stride anyway; they
-        // keep ceil(A/G), measured 1.5 % faster there.  Trailing threads may
-        // get short or empty runs.
+        // rows an odd stride puts the threads' record loads in distinct banks.
         const int M = ((A + G - 1) / G) | (G >= 64 ? 1 : 0);
+        int run_b, run_e, r0 = 0, r1 = 0;
+        if (aligned) {
+            r0 = row_bound(g, G, A, A1, h, P, T1, T2, inv1, inv2);
+            r1 = row_bound(g + 1, G, A, A1, h, P, T1, T2, inv1, inv2);
+            run_b = row_start(r0, h, A1, T1, T2);
+            run_e = row_start(r1, h, A1, T1, T2);
+        } else {
+            run_b = min(g * M, A);
+            run_e = min(run_b + M, A);
+        }
+        // the running sum after every pair is kept (transposed: element i of
+        // thread g at i*G + g) when every run of the group fits the buffer
+        const bool stored = sm.rates != nullptr &&
+                            static_cast<int>(grp.max_u32(static_cast<uint32_t>(run_e - run_b))) * G <= sm.rate_words;
         float lsum = 0.0f;
-        {
-            // The thread walks its contiguous run of pairs in row-major order,
-            // two pairs per step (two independent load -> rate chains; a row
-            // change is a select, not a branch).  When the shared-memory
-            // budget allows, the running sum after every pair is kept
-            // (transposed: element i of thread g at i*G + g) for the event
-            // search below.
-            const int kb = g * M;
-            const int ke = min(kb + M, A);
-            if (kb < ke) {
-                int row, col;
-                decode_pair(kb, h, A1, T1, T2, inv1, inv2, row, col);
-                KMC_DCHECK(ke <= A && row >= 0 && row < h + P && col >= 0 && col < (row < h ? T1 : T2));
-                KMC_DCHECK(!sm.rates || (M - 1) * G + g < sm.rate_cap);
-                bool sa = row < h;
-                int Tc = sa ? T1 : T2;
-                Rec sr = sm.src[row];
-                float *rp = sm.rates ? sm.rates + g : nullptr;
-                int k = kb;
+        float *rp = stored ? sm.rates + g : nullptr;
+        if (aligned) {
+            for (int row = r0; row < r1; ++row) {
+                KMC_DCHECK(row >= 0 && row < h + P);
+                const Rec sr = sm.src[row];
+                const bool sa = row < h;
+                const int Tc = sa ? T1 : T2;
+                int col = 0;
 #pragma unroll kPairUnroll
-                for (; k + 1 < ke; k += 2) {
-                    // second pair of the step
-                    const bool wa = (col + 1 == Tc);
-                    const int colb = wa ? 0 : col + 1;
-                    const int rowb = row + (wa ? 1 : 0);
-                    Rec srb = sr;
-                    if (wa) srb = sm.src[rowb];        // reload only on a row change
-                    const bool sab = rowb < h;
-                    const int Tcb = sab ? T1 : T2;
+                for (; col + 1 < Tc; col += 2) {
                     const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    const float rb = pairs.rate(srb, sm.tgt[colb], sab && colb < z, cs);
+                    const float rb = pairs.rate(sr, sm.tgt[col + 1], sa && col + 1 < z, cs);
                     lsum += ra;
-                    if (rp) { rp[0] = lsum; }
+                    if (rp) rp[0] = lsum;
                     lsum += rb;
                     if (rp) { rp[G] = lsum; rp += 2 * G; }
-                    // advance past the second pair
-                    const bool wb = (colb + 1 == Tcb);
-                    col = wb ? 0 : colb + 1;
-                    row = rowb + (wb ? 1 : 0);
-                    sr = srb;
-                    if (wb) sr = sm.src[row];
-                    sa = row < h;
-                    Tc = sa ? T1 : T2;
                 }
-                if (k < ke) {
+                if (col < Tc) {
                     lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    if (rp) rp[0] = lsum;
+                    if (rp) { rp[0] = lsum; rp += G; }
                 }
             }
+        } else if (run_b < run_e) {
+            // The thread walks its run in row-major order, two pairs per step
+            // (two independent load -> rate chains; a row change is a select
+            // plus a predicated reload, not a branch).
+            const int kb = run_b, ke = run_e;
+            int row, col;
+            decode_pair(kb, h, A1, T1, T2, inv1, inv2, row, col);
+            KMC_DCHECK(ke <= A && row >= 0 && row < h + P && col >= 0 && col < (row < h ? T1 : T2));
+            bool sa = row < h;
+            int Tc = sa ? T1 : T2;
+            Rec sr = sm.src[row];
+            int k = kb;
+#pragma unroll kPairUnroll
+            for (; k + 1 < ke; k += 2) {
+                // second pair of the step
+                const bool wa = (col + 1 == Tc);
+                const int colb = wa ? 0 : col + 1;
+                const int rowb = row + (wa ? 1 : 0);
+                Rec srb = sr;
+                if (wa) srb = sm.src[rowb];        // reload only on a row change
+                const bool sab = rowb < h;
+                const int Tcb = sab ? T1 : T2;
+                const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                const float rb = pairs.rate(srb, sm.tgt[colb], sab && colb < z, cs);
+                lsum += ra;
+                if (rp) { rp[0] = lsum; }
+                lsum += rb;
+                if (rp) { rp[G] = lsum; rp += 2 * G; }
+                // advance past the second pair
+                const bool wb = (colb + 1 == Tcb);
+                col = wb ? 0 : colb + 1;
+                row = rowb + (wb ? 1 : 0);
+                sr = srb;
+                if (wb) sr = sm.src[row];
+                sa = row < h;
+                Tc = sa ? T1 : T2;
+            }
+            if (k < ke) {
+                lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                if (rp) rp[0] = lsum;
+            }
         }
+        // the run [b, e) of thread l of the group
+        auto run_of = [&](int l, int &b, int &e) {
+            if (aligned) {
+                b = row_start(row_bound(l, G, A, A1, h, P, T1, T2, inv1, inv2), h, A1, T1, T2);
+                e = row_start(row_bound(l + 1, G, A, A1, h, P, T1, T2, inv1, inv2), h, A1, T1, T2);
+            } else {
+                b = min(l * M, A);
+                e = min(b + M, A);
+            }
+        };
         npairs += static_cast<unsigned long long>(A);
         KMC_SECTION(1);
         // ---- uniforms for this hop ----
@@ -943,7 +1024,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             u_ev = grp.bcast(rnd_u, ri);
 #endif
         }
-        if (sm.rates) grp.sync();   // stored rates visible to the whole group
+        if (stored) grp.sync();   // stored rates visible to the whole group
         KMC_SECTION(2);
 #ifdef KMC_SELECT_DOUBLE_FLOAT
         // ---- double-float scan of the per-thread sums ----
@@ -953,7 +1034,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         const float totf = tot.hi;
         const F2 target = df_mul(u_ev, tot);
         int L = grp.first(df_ge(incl, target));
-        if (L < 0) L = (A - 1) / M;   // u*total rounded above the total: the last non-empty run
+        if (L < 0) L = grp.last(run_e > run_b);   // u*total rounded above the total: the last non-empty run
         const F2 baseL = grp.bcast2(excl, L);
         float rem = df_add(target, F2{-baseL.hi, -baseL.lo}).hi;
 #else
@@ -972,7 +1053,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         // thread L's run holds it (tot >= target, so some thread qualifies)
         const uint64_t target = fixed_target(u_ev, tot);
         int L = grp.first(incl >= target);
-        if (L < 0) L = (A - 1) / M;
+        if (L < 0) L = grp.last(run_e > run_b);
         // what remains of u*total beyond the runs before L, back in FP32
         float rem = grp.bcast(from_fixed(target - excl, emax, kShift), L);
 #endif
@@ -980,11 +1061,13 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         // ---- find the event inside thread L's run ----
         int chosen = -1, last_pos = -1;
         if (!(rem > 0.0f)) rem = 1.0e-38f;   // first pair with a positive rate
-        if (sm.rates) {
+        int kbL, keL;
+        run_of(L, kbL, keL);
+        if (stored) {
             // Thread L kept its running sums: the event is the first pair whose
             // sum reaches rem.  Each thread of the group searches one block of
             // them; the lowest block with a hit wins.
-            const int len = min(M, A - L * M);
+            const int len = keL - kbL;
             const int Bk = (len + G - 1) / G;
             const int i0 = g * Bk, i1 = min(i0 + Bk, len);
             int found = -1;
@@ -992,7 +1075,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 if (sm.rates[i * G + L] >= rem) { found = i; break; }
             const int hl = grp.first(found >= 0);
             if (hl >= 0) {
-                chosen = L * M + grp.bcast(found, hl);
+                chosen = kbL + grp.bcast(found, hl);
             } else if (len > 0) {
                 // rem rounded above the run's total: the run's last pair
                 // with a positive rate
@@ -1000,12 +1083,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 for (int i = i0; i < i1; ++i)
                     if (sm.rates[i * G + L] > (i > 0 ? sm.rates[(i - 1) * G + L] : 0.0f)) lp = i;
                 const int ll = grp.last(lp >= 0);
-                if (ll >= 0) chosen = L * M + grp.bcast(lp, ll);
+                if (ll >= 0) chosen = kbL + grp.bcast(lp, ll);
             }
         } else {
-            const int kb = L * M;
-            const int ke = min(kb + M, A);
-            const int len = ke - kb;
+            const int kb = kbL;
+            const int len = keL - kbL;
             for (int i0 = 0; i0 < len; i0 += G) {
                 const int i = i0 + g;
                 float r = 0.0f;
@@ -1027,17 +1109,19 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (chosen < 0) chosen = last_pos;
         if (chosen < 0) { status = KMC_ERR_NONFINITE; break; }
 #if defined(KMC_DEBUG_CHECKS) && !defined(KMC_SELECT_DOUBLE_FLOAT)
-        if (B.select_mismatch && sm.rates) {
+        if (B.select_mismatch && stored) {
             // the same selection with an FP64 scan and compare over the same
             // FP32 per-thread sums: count the hops where it picks another pair
             double dex, dtot;
             const double dinc = grp.scan_f64(static_cast<double>(lsum), dex, dtot);
             const double dtarget = __ull2double_rn(u_ev) * 0x1.0p-64 * dtot;
             int L64 = grp.first(dinc >= dtarget);
-            if (L64 < 0) L64 = (A - 1) / M;
+            if (L64 < 0) L64 = grp.last(run_e > run_b);
             const float rem64 = grp.bcast(static_cast<float>(dtarget - dex), L64);
             if (g == 0) {
-                const int len = min(M, A - L64 * M);
+                int kb64, ke64;
+                run_of(L64, kb64, ke64);
+                const int len = ke64 - kb64;
                 int c64 = -1, lp = -1;
                 for (int i = 0; i < len; ++i) {
                     const float ri = sm.rates[i * G + L64];
@@ -1045,12 +1129,12 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     if (ri > (i > 0 ? sm.rates[(i - 1) * G + L64] : 0.0f)) lp = i;
                 }
                 if (c64 < 0) c64 = lp;
-                if (L64 * M + c64 != chosen) B.select_mismatch[c] += 1ull;
+                if (kb64 + c64 != chosen) B.select_mismatch[c] += 1ull;
             }
         }
 #endif
         int row, col;
-        KMC_DCHECK(chosen >= 0 && chosen < A && L >= 0 && L < G);
+        KMC_DCHECK(chosen >= 0 && chosen < A && L >= 0 && L < G && chosen >= kbL && chosen < keL);
         decode_pair(chosen, h, A1, T1, T2, inv1, inv2, row, col);
         KMC_DCHECK(row >= 0 && row < h + P && col >= 0 && col < (row < h ? T1 : T2));
 #ifdef KMC_DEBUG_CHECKS
