@@ -885,12 +885,15 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         // g*A/G, so every thread starts each row at column 0: the threads of a
         // group read the same target record at the same time (one broadcast
         // load) and need no per-pair row bookkeeping, at the price of runs up
-        // to one row longer than A/G.  Row-aligned runs pay off when a run
-        // spans at least 1.5 rows.
+        // to one row longer than A/G and a loop set-up per row.  Measured on
+        // GB300: +46 % on N=1000 networks (rows of ~108 targets, 256
+        // threads), -26 % on the N=30 ensemble (rows of 11): row-aligned runs
+        // are taken for rows of at least 32 targets and runs of at least 1.5
+        // rows.
 #ifdef KMC_FORCE_BALANCED_RUNS
         const bool aligned = false;   // measurement builds: the balanced split only
 #else
-        const bool aligned = A >= ((3 * G * T1) >> 1);
+        const bool aligned = T1 >= 32 && A >= ((3 * G * T1) >> 1);
 #endif
         // Balanced run length.  Block groups round it up to an odd number:
         // thread g's run starts M records after thread g-1's, and with long
@@ -909,7 +912,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         // the running sum after every pair is kept (transposed: element i of
         // thread g at i*G + g) when every run of the group fits the buffer
         const bool stored = sm.rates != nullptr &&
-                            static_cast<int>(grp.max_u32(static_cast<uint32_t>(run_e - run_b))) * G <= sm.rate_words;
+                            (aligned ? static_cast<int>(grp.max_u32(static_cast<uint32_t>(run_e - run_b))) * G
+                                     : M * G) <= sm.rate_words;
         float lsum = 0.0f;
         float *rp = stored ? sm.rates + g : nullptr;
         if (aligned) {
