@@ -886,15 +886,18 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         // group read the same target record at the same time (one broadcast
         // load) and need no per-pair row bookkeeping, at the price of runs up
         // to one row longer than A/G and a loop set-up per row.  Measured on
-        // GB300: +46 % on N=1000 networks (rows of ~108 targets, 256
-        // threads), -26 % on the N=30 ensemble (rows of 11): row-aligned runs
-        // are taken for rows of at least 32 targets and runs of at least 1.5
-        // rows.
+        // GB300: +47 % on N=1000 networks (rows of ~108 targets, block groups
+        // of 256 threads), -26 % on the N=30 ensemble (rows of 11, warp
+        // slices), and even compiled in but not taken it cost the warp-slice
+        // kernels 3 %: block groups take row-aligned runs for rows of at
+        // least 32 targets and runs of at least 1.5 rows; warp slices are
+        // compiled with balanced runs only.
 #ifdef KMC_FORCE_BALANCED_RUNS
-        const bool aligned = false;   // measurement builds: the balanced split only
+        constexpr bool kAlignedRuns = false;   // measurement builds: the balanced split only
 #else
-        const bool aligned = T1 >= 32 && A >= ((3 * G * T1) >> 1);
+        constexpr bool kAlignedRuns = G >= 64;
 #endif
+        const bool aligned = kAlignedRuns && T1 >= 32 && A >= ((3 * G * T1) >> 1);
         // Balanced run length.  Block groups round it up to an odd number:
         // thread g's run starts M records after thread g-1's, and with long
         // rows an odd stride puts the threads' record loads in distinct banks.
