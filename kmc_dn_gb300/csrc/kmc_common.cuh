@@ -39,6 +39,15 @@ __device__ __forceinline__ float u01_from32(uint32_t x)
     return (static_cast<float>(x >> 9) + 0.5f) * (1.0f / 8388608.0f);
 }
 
+// Uniform in (0,1] for the clock's exponential variate: (x + 1/2) 2^-32
+// rounded to FP32.  Near 0, where -log u is large, FP32 keeps every one of
+// the 32 bits, so -log u reaches ln(2^33) = 22.9 and the exponential tail
+// beyond it (mean weight e^-22.9 = 1e-10) is all that is cut.
+__device__ __forceinline__ float u01_tail32(uint32_t x)
+{
+    return fmaf(static_cast<float>(x), 0x1.0p-32f, 0x1.0p-33f);
+}
+
 // Uniform in (0,1) with 53 random bits from two words.
 __device__ __forceinline__ double u01_from64(uint32_t hi, uint32_t lo)
 {

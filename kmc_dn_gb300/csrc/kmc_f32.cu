@@ -1016,7 +1016,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                                                     static_cast<uint32_t>(stream),
                                                     static_cast<uint32_t>(stream >> 32)},
                                               k0, k1);
-                rnd_e1 = -__logf(u01_from32(w.x));
+                // Exp(1) clock variate: logf (within an ulp; once per G hops
+                // per thread) of a 32-bit uniform
+                rnd_e1 = -logf(u01_tail32(w.x));
 #ifdef KMC_SELECT_DOUBLE_FLOAT
                 rnd_u = u01_df(w.y, w.z);
 #else
@@ -1512,6 +1514,20 @@ int launch_block(const kmc_batch &b, cudaStream_t st)
     const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
     int rw = rate_buffer_words(b.max_sites, T);
     if (static_cast<size_t>(lw + rw) * 4 > kSmemBudget) rw = 0;
+    if (rw > 0) {
+        // Without the running-sum buffer the event search re-evaluates the
+        // chosen thread's run, for a block group a chunk or two of rates.
+        // Drop the buffer when it is what limits the blocks an SM holds and
+        // the launch has more chains than the SMs then hold at once (a
+        // 512-chain request of N=240 networks at 512 threads: one wave of
+        // blocks instead of two).
+        const int per_sm_threads = 2048 / T;
+        const int per_sm_with = static_cast<int>((227 * 1024) / (static_cast<size_t>(lw + rw) * 4));
+        const int per_sm_without = static_cast<int>((227 * 1024) / (static_cast<size_t>(lw) * 4));
+        if (per_sm_with < per_sm_threads && per_sm_without > per_sm_with &&
+            b.n_work > per_sm_with * sm_count())
+            rw = 0;
+    }
     const size_t chain = static_cast<size_t>(lw + rw) * 4;
     const int tw = table_stage_words<Pairs>(b, chain);
     const size_t smem = chain + static_cast<size_t>(tw) * 4;
