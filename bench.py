@@ -209,6 +209,7 @@ def accuracy_of(cases, dev, replicas32=512, replicas64=128, hops=300_000, seed=0
     tf64 = time.perf_counter() - t0
     assert np.all(st64 == 0)
     cnt, cv, above, betas, vr, ozs, odiff = {"z": [], "rel": [], "up": []}, {"z": [], "rel": [], "up": []}, [], [], [], [], []
+    per_current = []
     for c in range(len(cases)):
         i32 = [i for i, rc in enumerate(rows) if rc == c]
         i64 = [i for i, rc in enumerate(rows64) if rc == c]
@@ -227,6 +228,8 @@ def accuracy_of(cases, dev, replicas32=512, replicas64=128, hops=300_000, seed=0
         cnt["z"].append(z), cnt["rel"].append(rel), cnt["up"].append(up)
         _, se_v, z, rel, up = _current_stats(C32 - beta * D32, C64 - beta * D64)
         cv["z"].append(z), cv["rel"].append(rel), cv["up"].append(up)
+        per_current.extend([c, e, float(m64[e]), round(float(rel[e]), 5), round(float(up[e]), 5)]
+                           for e in range(len(m64)) if abs(m64[e]) >= FLOOR * np.abs(m64).max())
         vr.append((se_c / np.maximum(se_v, 1e-300)) ** 2)
         above.append(np.abs(m64) >= FLOOR * np.abs(m64).max())
         O32 = np.stack([r32["occ_time"][i] / r32["time"][i] for i in i32])
@@ -247,7 +250,10 @@ def accuracy_of(cases, dev, replicas32=512, replicas64=128, hops=300_000, seed=0
             "control_variate_estimate": dict(_summary(catv["z"], catv["rel"], catv["up"], ab),
                                              median_variance_reduction=float(np.median(np.concatenate(vr))),
                                              beta_range=[float(np.concatenate(betas).min()),
-                                                         float(np.concatenate(betas).max())]),
+                                                         float(np.concatenate(betas).max())],
+                                             above_floor=dict(columns=["vector", "electrode", "I_fp64",
+                                                                       "rel_diff", "rel_upper3"],
+                                                              rows=per_current)),
             "occupancies": int(oz.size), "occupancy_max_abs_z": float(oz.max()),
             "occupancy_frac_within_3sigma": float(np.mean(oz <= 3.0)),
             "occupancy_max_abs_diff": float(od.max()),

@@ -103,3 +103,49 @@ def test_engine_follows_fp64_hop_sequence_large_network(engine_lib, lanes, pair_
     net, u, o, _ = _reference(300, hops, 78)
     r = _engine(net, u, hops, lanes, pair_mode)
     _check(net, o, r, hops, f"N=300 G={lanes} {pair_mode}")
+
+
+def _uneven_cases():
+    """Three networks of the uneven workload's distributions with temperatures
+    and localisation lengths far from 1 (kT 0.5..5, ab/R 0.5..2) and 4 to 12
+    electrodes."""
+    from kmc_dn_gb300 import workloads
+    nets = [n for n, _ in workloads.uneven_batch(64, seed=123, hops_range=(1000, 1000))]
+    lo = min(nets, key=lambda n: n.kT)
+    hi = max(nets, key=lambda n: n.kT)
+    wide = max(nets, key=lambda n: n.ab / n.R)
+    return [lo, hi, wide]
+
+
+@functools.lru_cache(maxsize=None)
+def _uneven_reference(k, hops, seed):
+    import oracle as orc
+    net = _uneven_cases()[k]
+    occ = net.occupation.astype(np.uint8)
+    u, _ = orc.clear_stream(net.N, net.P, net.nu, net.kT, net.I_0, net.R, occ, net.distances, net.E_constant(),
+                            net.site_energies(), net.transitions_constant, hops, seed, MARGIN)
+    o = orc.numba_replay(net.N, net.P, net.nu, net.kT, net.I_0, net.R, occ, net.distances, net.E_constant(),
+                         net.site_energies(), net.transitions_constant, u, record=True)
+    return net, u, o
+
+
+@pytest.mark.parametrize("k", [0, 1, 2], ids=["coldest", "hottest", "widest_ab"])
+@pytest.mark.parametrize("pair_mode", ["table", "positions"])
+def test_engine_follows_fp64_on_uneven_networks(engine_lib, k, pair_mode):
+    """Networks with kT from 0.5 to 5 and ab/R from 0.5 to 2: 10^4 hops of a
+    boundary-clear stream identical to the FP64 loop's, at the default lanes
+    for their size, in both pair modes."""
+    from kmc_dn_gb300.engine import default_lanes
+    hops = 10_000
+    net, u, o = _uneven_reference(k, hops, 90 + k)
+    r = _engine(net, u, hops, default_lanes(net.S), pair_mode)
+    assert r["status"][0] == 0
+    mism = np.flatnonzero(np.any(r["hop_log"][0] != o["hop_log"], axis=1))
+    assert mism.size == 0, f"N={net.N} kT={net.kT:.2f}: first divergence at hop {mism[0]}"
+    np.testing.assert_array_equal(r["electrode_occupation"][0], o["electrode_occupation"])
+    np.testing.assert_array_equal(r["occupation"][0], o["occupation"].astype(bool))
+    rates = r["hop_rates"][0].astype(np.float64)
+    p32 = rates[:, 1] / rates[:, 0]
+    p64 = o["hop_rates"] / o["hop_totals"]
+    assert np.max(np.abs(rates[:, 0] / o["hop_totals"] - 1.0)) <= 2e-3
+    assert np.max(np.abs(p32 / p64 - 1.0)) <= 5e-3
