@@ -1077,22 +1077,30 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             // sum reaches rem.  Each thread of the group searches one block of
             // them; the lowest block with a hit wins.
             const int len = keL - kbL;
-            const int Bk = (len + G - 1) / G;
-            const int i0 = g * Bk, i1 = min(i0 + Bk, len);
-            int found = -1;
-            for (int i = i0; i < i1; ++i)
-                if (sm.rates[i * G + L] >= rem) { found = i; break; }
-            const int hl = grp.first(found >= 0);
-            if (hl >= 0) {
-                chosen = kbL + grp.bcast(found, hl);
+            // Thread g tests elements g, g + G, ... of thread L's run, a chunk
+            // of G elements per round with both rounds' loads issued first;
+            // the running sums do not decrease, so the lowest element of the
+            // first chunk with a hit is the event.
+            int idx = -1;
+            for (int i0 = 0; i0 < len && idx < 0; i0 += 2 * G) {
+                const int ia = i0 + g, ib = i0 + G + g;
+                const float va = ia < len ? sm.rates[ia * G + L] : -1.0f;
+                const float vb = ib < len ? sm.rates[ib * G + L] : -1.0f;
+                const int ha = grp.first(va >= rem);
+                const int hb = grp.first(vb >= rem);
+                if (ha >= 0) idx = i0 + ha;
+                else if (hb >= 0) idx = i0 + G + hb;
+            }
+            if (idx >= 0) {
+                chosen = kbL + idx;
             } else if (len > 0) {
                 // rem rounded above the run's total: the run's last pair
                 // with a positive rate
                 int lp = -1;
-                for (int i = i0; i < i1; ++i)
+                for (int i = g; i < len; i += G)
                     if (sm.rates[i * G + L] > (i > 0 ? sm.rates[(i - 1) * G + L] : 0.0f)) lp = i;
-                const int ll = grp.last(lp >= 0);
-                if (ll >= 0) chosen = kbL + grp.bcast(lp, ll);
+                const int ll = static_cast<int>(grp.max_u32(static_cast<uint32_t>(lp + 1))) - 1;
+                if (ll >= 0) chosen = kbL + ll;
             }
         } else {
             const int kb = kbL;
