@@ -262,10 +262,26 @@ def accuracy_of(cases, dev, replicas32=512, replicas64=128, hops=300_000, seed=0
             "fp64_s": tf64}
 
 
+def energy_drift(net, V, dev, n_chains=512, hops=100_000, seed=0):
+    """Largest difference (kT) between the engine's incrementally updated
+    FP32 energies and their recomputation at the re-anchors (every 1024
+    hops), over n_chains chains of the homogeneous workload."""
+    from kmc_dn_gb300.engine import Batch, TableSpec, superpose
+    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    ec, ve = superpose(net.basis, net.comp, V[:n_chains], net.mu, dev=dev)
+    b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT), None, None,
+              np.tile(net.occupation.astype(np.uint8), (n_chains, 1)), np.full(n_chains, hops), seed=seed + 3,
+              lanes=16, dev=dev, E_constant_dev=ec, el_energy_dev=ve, measure_drift=True)
+    r = b.run().results()
+    return {"chains": n_chains, "hops": hops, "reanchor": 1024, "max": float(r["energy_drift"].max()),
+            "median": float(np.median(r["energy_drift"]))}
+
+
 def accuracy_sample(net, V, dev, n_vectors=16, replicas32=512, replicas64=128, hops=300_000, seed=0):
     """``accuracy_of`` on the first ``n_vectors`` voltage vectors of the
-    homogeneous workload."""
+    homogeneous workload, and the energy drift its chains see."""
     out = accuracy_of([(net, V[k]) for k in range(n_vectors)], dev, replicas32, replicas64, hops, seed)
+    out["energy_drift_kT"] = energy_drift(net, V, dev, seed=seed)
     out["reference"] = ("plain FP64 kernel (bit-exact to the reference loop's hop sequence), "
                         "independent replicas")
     return out

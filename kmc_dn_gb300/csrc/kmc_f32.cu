@@ -790,6 +790,17 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // last anchor are compared with the recomputed ones first, and the
     // largest difference (in units of kT) is kept per chain.
     float drift_max = 0.0f;
+    // Compensated energies (TwoSum per increment) in block groups, where
+    // networks are large and hundreds of terms per hop would otherwise let
+    // the FP32 energies drift by up to 0.02 kT between re-anchors (measured
+    // on N=1000 networks); warp slices run small networks whose drift stays
+    // near 1e-3 kT and keep one add per increment (the compensation cost
+    // 2.5 % of the N=30 ensemble's throughput).
+    constexpr bool kComp = G >= 64;
+    auto eadd = [](float &hi, float &lo, float c) {
+        if (kComp) comp_add(hi, lo, c);
+        else hi += c;
+    };
     // The record of electrode g (thread g < P), the same every hop of the
     // launch: the rebuilds after a hop copy it instead of reading the
     // electrode's energy from global memory again.
@@ -799,10 +810,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             // E_j = Ec_j - sum_{k empty} B_jk, summed with compensation
             float hi = Ec[j], lo = 0.0f;
             for (int k = 0; k < N; ++k)
-                if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) comp_add(hi, lo, -pairs.coulomb(j, k));
-            if (drift) drift_max = fmaxf(drift_max, fabsf((hi - sm.E[j]) + (lo - sm.Elo[j])));
+                if (!((sm.occw[k >> 5] >> (k & 31)) & 1u)) eadd(hi, lo, -pairs.coulomb(j, k));
+            if (drift) drift_max = fmaxf(drift_max, fabsf((hi - sm.E[j]) + (lo - (kComp ? sm.Elo[j] : 0.0f))));
             sm.E[j] = hi;
-            sm.Elo[j] = lo;
+            if (kComp) sm.Elo[j] = lo;
         }
         const int z = N - h;
         int wcur = 0, cum = 0;
@@ -811,7 +822,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
             const uint32_t word = sm.occw[w];
             const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
-            const Rec r = pairs.rec(j, cs * (sm.E[j] + sm.Elo[j]));
+            const Rec r = pairs.rec(j, cs * (kComp ? sm.E[j] + sm.Elo[j] : sm.E[j]));
             if ((word >> (j & 31)) & 1u) {
                 sm.src[below] = r;
                 if (!Pairs::kSiteInRec) sm.src_id[below] = j;
@@ -1203,11 +1214,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             int wcur = 0, cum = 0;
             for (int j = g; j < N; j += G) {
                 // O(N) update (makeJump, simulation.go:107-130), compensated
-                float Ej = sm.E[j], Elo = sm.Elo[j];
-                if (fa && j != from) comp_add(Ej, Elo, -pairs.coulomb(j, from));
-                if (tb && j != to) comp_add(Ej, Elo, pairs.coulomb(j, to));
+                float Ej = sm.E[j], Elo = kComp ? sm.Elo[j] : 0.0f;
+                if (fa && j != from) eadd(Ej, Elo, -pairs.coulomb(j, from));
+                if (tb && j != to) eadd(Ej, Elo, pairs.coulomb(j, to));
                 sm.E[j] = Ej;
-                sm.Elo[j] = Elo;
+                if (kComp) sm.Elo[j] = Elo;
                 const int w = j >> 5;
                 while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
                 const uint32_t word = sm.occw[w];
@@ -1221,7 +1232,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     continue;
                 }
 #endif
-                const Rec r = pairs.rec(j, cs * (Ej + Elo));
+                const Rec r = pairs.rec(j, cs * (kComp ? Ej + Elo : Ej));
                 if (occ_j) {
                     sm.src[below] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[below] = j;
