@@ -314,6 +314,10 @@ typedef struct kmc_batch {
      * stay resident), so that launches of several size bins running side by
      * side can share the device in proportion to their work */
     int32_t max_grid;
+    /* > 0: every chain of the launch has this kT (the engine then stages a
+     * single pair table with the temperature folded in; a chain whose kT
+     * differs stops with KMC_ERR_INVALID).  0: per-chain kT as given */
+    float uniform_kT;
 } kmc_batch;
 
 /*

@@ -64,7 +64,7 @@ class KmcBatch(C.Structure):
         ("time_budget_ns", _i64),
         ("hop_log", _vp), ("hop_rates", _vp), ("hop_log_off", _vp), ("select_mismatch", _vp),
         ("energy_drift", _vp), ("work_counter", _vp), ("flux_time", _vp),
-        ("max_grid", _i32),
+        ("max_grid", _i32), ("uniform_kT", C.c_float),
     ]
 
 

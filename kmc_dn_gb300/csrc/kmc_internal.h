@@ -19,6 +19,14 @@ int fail_cuda(cudaError_t e, const char *what);
 int ok();
 
 int run_batch(const kmc_batch &b, cudaStream_t st);
+// engine launches by group kind and pair mode (kmc_f32_*.cu)
+int launch_warp_table(const kmc_batch &b, cudaStream_t st);
+int launch_warp_positions(const kmc_batch &b, cudaStream_t st);
+int launch_block_table(const kmc_batch &b, cudaStream_t st);
+int launch_block_positions(const kmc_batch &b, cudaStream_t st);
+int section_clocks_warp_table(uint64_t *out, int reset);
+int section_clocks_warp_positions(uint64_t *out, int reset);
+int section_clocks_block(uint64_t *out, int reset);
 // Per-phase cycle counters of a -DKMC_SECTION_CLOCKS build (9 values).
 int section_clocks(uint64_t *out, int reset);
 int engine_smem_words(int max_sites);

@@ -457,7 +457,10 @@ class Batch:
         self.el_energy = el_energy_dev if el_energy_dev is not None else pool(el_energy, nel, torch.float32, np.float32)
         self.occupation = pool(occupation, nsite, torch.uint8, np.uint8)
         self.chain_tab_d = _dev(ct, torch.int32, d)
-        self.kT = _dev(np.broadcast_to(np.asarray(kT, np.float32), (n,)), torch.float32, d)
+        kT32 = np.broadcast_to(np.asarray(kT, np.float32), (n,))
+        self.kT = _dev(kT32, torch.float32, d)
+        # one temperature for every chain: the engine may fold it into a staged table
+        self.uniform_kT = float(kT32[0]) if n and np.all(kT32 == kT32[0]) else 0.0
         self.site_off_d = _dev(self.site_off, torch.int64, d)
         self.el_off_d = _dev(self.el_off, torch.int64, d)
         self.pair_off_d = _dev(self.pair_off, torch.int64, d)
@@ -565,6 +568,7 @@ class Batch:
         if self.cancel is not None:
             b.cancel = self.cancel.device
         b.time_budget_ns = int(self.time_budget_ns)
+        b.uniform_kT = self.uniform_kT
         if self.select_mismatch is not None:
             b.select_mismatch = self.select_mismatch.data_ptr()
         if self.energy_drift is not None:

@@ -465,3 +465,20 @@ def test_f64_batch_launch_equals_single_chain_runs(engine_lib):
         np.testing.assert_array_equal(r["electrode_occupation"], eo[k])
         np.testing.assert_array_equal(r["occupations_in_time"], oit[k])
         np.testing.assert_array_equal(r["flux_time"], fx[k])
+
+
+def test_uniform_temperature_table_guards_its_chains(engine_lib):
+    """A launch whose chains share one kT stages its pair table with the
+    temperature folded in; a chain whose kT differs from the launch's
+    uniform_kT stops with KMC_ERR_INVALID instead of using that table."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300._native import KMC_ERR_INVALID
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    n = workloads.plain_network(0)
+    spec = TableSpec(n.N, n.P, n.nu, n.I_0, n.R, n.distances, n.transitions_constant)
+    b = Batch([spec], [0, 0], [1.0, 1.0], [n.E_constant()] * 2, [n.electrodes[:, 3]] * 2,
+              [n.occupation.astype(np.uint8)] * 2, [2048, 2048], lanes=16)
+    assert b.uniform_kT == 1.0
+    b.uniform_kT = 0.75                     # as if the table were staged for another kT
+    r = b.run().results()
+    assert np.all(r["status"] == KMC_ERR_INVALID) and np.all(r["hops_done"] == 0)
