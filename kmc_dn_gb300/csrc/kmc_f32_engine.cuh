@@ -302,15 +302,12 @@ __device__ __forceinline__ void decode_pair(int k, int h, int A1, int T1, int T2
 // Every variant evaluates the same expression,
 //     rate = 2^min(L, (L + c B) - (e_t - e_s)),  L + c B = fma(c, B, L),
 // so a chain's result does not depend on which one runs it.
-// A source record carries its table row's byte offset (site * S * 8), a
-// target record its column's (site * 8), so a pair's table entry is one
-// three-input add away; the site ids are kept beside the records.
 template <bool kStaged, bool kUniform = false>
 struct TablePairs {
     using Rec = int2;
-    static constexpr bool kSiteInRec = false;   // site ids kept beside the records
+    static constexpr bool kSiteInRec = true;    // rec.x is the site id
     static constexpr bool kUniformTable = kUniform;
-    __device__ __forceinline__ static int site(Rec) { return -1; }
+    __device__ __forceinline__ static int site(Rec r) { return r.x; }
     const float2 *tab;
     const float *coul;   // kUniform: B of each pair
     int S;
@@ -323,14 +320,10 @@ struct TablePairs {
         S = S_;
         coul = kUniform ? reinterpret_cast<const float *>(shared_tab + S_ * S_) : nullptr;
     }
-    __device__ __forceinline__ Rec rec_src(int site, float e) const
-    {
-        return make_int2(site * S * 8, __float_as_int(e));
-    }
-    __device__ __forceinline__ Rec rec_tgt(int site, float e) const { return make_int2(site * 8, __float_as_int(e)); }
+    __device__ __forceinline__ Rec rec(int site, float e) const { return make_int2(site, __float_as_int(e)); }
     __device__ __forceinline__ float rate(Rec s, Rec t, bool /*acc*/, float cs) const
     {
-        const float2 lb = *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(tab) + (s.x + t.x));
+        const float2 lb = tab[s.x * S + t.x];
         const float d = __int_as_float(t.y) - __int_as_float(s.y);
         const float lcb = kUniform ? lb.y : fmaf(cs, lb.y, lb.x);
         return ex2_approx(fminf(lb.x, lcb - d));
@@ -363,8 +356,6 @@ struct PositionPairs {
         const float4 p = __ldg(&pos[site]);
         return make_float4(p.x, p.y, p.z, e);
     }
-    __device__ __forceinline__ Rec rec_src(int site, float e) const { return rec(site, e); }
-    __device__ __forceinline__ Rec rec_tgt(int site, float e) const { return rec(site, e); }
     __device__ __forceinline__ float rate(Rec s, Rec t, bool acc, float cs) const
     {
         const float dx = t.x - s.x, dy = t.y - s.y, dz = t.z - s.z;
@@ -765,7 +756,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
     // The record of electrode g (thread g < P), the same every hop of the
     // launch: the rebuilds after a hop copy it instead of reading the
     // electrode's energy from global memory again.
-    Rec el_src{}, el_tgt{};
+    Rec el_rec{};
     auto anchor_and_build = [&](bool drift) {
         for (int j = g; j < N; j += G) {
             // E_j = Ec_j - sum_{k empty} B_jk, summed with compensation
@@ -783,23 +774,20 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             while (wcur < w) { cum += __popc(sm.occw[wcur]); ++wcur; }
             const uint32_t word = sm.occw[w];
             const int below = cum + __popc(word & ((1u << (j & 31)) - 1u));
-            const float ej = cs * (kComp ? sm.E[j] + sm.Elo[j] : sm.E[j]);
+            const Rec r = pairs.rec(j, cs * (kComp ? sm.E[j] + sm.Elo[j] : sm.E[j]));
             if ((word >> (j & 31)) & 1u) {
-                sm.src[below] = pairs.rec_src(j, ej);
+                sm.src[below] = r;
                 if (!Pairs::kSiteInRec) sm.src_id[below] = j;
             } else {
-                sm.tgt[j - below] = pairs.rec_tgt(j, ej);
+                sm.tgt[j - below] = r;
                 if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
             }
         }
         for (int e = g; e < P; e += G) {
-            const Rec rs = pairs.rec_src(N + e, cs * Vel[e]), rt = pairs.rec_tgt(N + e, cs * Vel[e]);
-            if (e == g) {   // kept for the list rebuilds of later hops
-                el_src = rs;
-                el_tgt = rt;
-            }
-            sm.src[h + e] = rs;
-            sm.tgt[z + e] = rt;
+            const Rec r = pairs.rec(N + e, cs * Vel[e]);
+            if (e == g) el_rec = r;   // kept for the list rebuilds of later hops
+            sm.src[h + e] = r;
+            sm.tgt[z + e] = r;
             if (!Pairs::kSiteInRec) {
                 sm.src_id[h + e] = N + e;
                 sm.tgt_id[z + e] = N + e;
@@ -1127,10 +1115,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             // a zero-mean martingale), a low-variance companion estimate of
             // the current for accuracy checks.
             for (int e = 0; e < P; ++e) {
-                const Rec es = sm.src[h + e], et = sm.tgt[z + e];   // electrode e as source, as target
+                const Rec er = sm.src[h + e];
                 float part = 0.0f;
                 for (int k = g; k < N; k += G)
-                    part += (k < h) ? pairs.rate(sm.src[k], et, false, cs) : -pairs.rate(es, sm.tgt[k - h], false, cs);
+                    part += (k < h) ? pairs.rate(sm.src[k], er, false, cs) : -pairs.rate(er, sm.tgt[k - h], false, cs);
                 const float J = grp.sumf(part);
                 if (g == 0) B.flux_time[eoff + e] += static_cast<double>(J) * static_cast<double>(dt);
             }
@@ -1163,20 +1151,21 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     continue;
                 }
 #endif
-                const float ej = cs * (kComp ? Ej + Elo : Ej);
+                const Rec r = pairs.rec(j, cs * (kComp ? Ej + Elo : Ej));
                 if (occ_j) {
-                    sm.src[below] = pairs.rec_src(j, ej);
+                    sm.src[below] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[below] = j;
                 } else {
-                    sm.tgt[j - below] = pairs.rec_tgt(j, ej);
+                    sm.tgt[j - below] = r;
                     if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
                 }
             }
             if (h_new != h) {
                 for (int e = g; e < P; e += G) {
-                    sm.src[h_new + e] = (e == g) ? el_src : pairs.rec_src(N + e, cs * Vel[e]);
+                    const Rec r = (e == g) ? el_rec : pairs.rec(N + e, cs * Vel[e]);
+                    sm.src[h_new + e] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[h_new + e] = N + e;
-                    sm.tgt[z_new + e] = (e == g) ? el_tgt : pairs.rec_tgt(N + e, cs * Vel[e]);
+                    sm.tgt[z_new + e] = r;
                     if (!Pairs::kSiteInRec) sm.tgt_id[z_new + e] = N + e;
                 }
             }
