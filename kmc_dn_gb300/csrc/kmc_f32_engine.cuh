@@ -109,7 +109,9 @@ inline int section_clocks_read(uint64_t *out, int reset)
 #endif
 // Unroll of the pair walk (four steps = eight pairs in flight per thread):
 // on the N=30 ensemble 10 % faster than no unrolling and 5 % faster than two
-// steps; the large networks are insensitive to it.
+// steps; the large networks are insensitive to it.  Steps of four or eight
+// pairs with all their loads issued before the running-sum stores measured
+// 1-2.5 % slower than two-pair steps.
 constexpr int kPairUnroll = KMC_PAIR_UNROLL;
 
 __device__ __forceinline__ float ex2_approx(float x)
@@ -634,13 +636,27 @@ __host__ __device__ __forceinline__ int chain_list_words(int S)
     return (words + 3) & ~3;
 }
 
+#ifndef KMC_RATE_PAD
+#define KMC_RATE_PAD 1
+#endif
+// Row stride of the stored running sums: element i of thread g of a G-thread
+// group sits at i*(G + 1) + g.  The threads store row i together (one
+// conflict-free wavefront), and the search, where thread g reads element g of
+// one thread's column, hits G distinct banks (with a stride of G it would hit
+// 32/gcd(G, 32) banks: 8-way conflicts for G = 16).
+template <int G>
+struct RateStride {
+    static constexpr int kValue = G + KMC_RATE_PAD;
+};
+
 // Words to keep every pair rate of one hop: A(h) <= S^2/3 for any split of
 // S sites into acceptors and electrodes; the transposed layout (element i of
-// thread g at i*G + g, i < M) reaches G*M <= A + 2G - 1 with M rounded up to
-// odd.
+// thread g at i*(G + 1) + g, i < M) reaches (G + 1)*M <= A + A/G + 2G + 2
+// with M <= A/G + 2 (rounded up to odd).
 __host__ __device__ __forceinline__ int rate_buffer_words(int S, int G)
 {
-    return (((S * S) / 3 + 1 + 2 * G) + 3) & ~3;
+    const int A = (S * S) / 3 + 1;
+    return ((A + A / G + 2 * G + 2) + 3) & ~3;
 }
 
 template <typename Rec>
@@ -672,6 +688,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                           int c, const float2 *shared_tab)
 {
     constexpr int G = Grp::kSize;
+    constexpr int RS = RateStride<G>::kValue;
     using Rec = typename Pairs::Rec;
     const int g = grp.g;
     const int t_id = B.chain_tab[c];
@@ -872,10 +889,10 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             run_e = min(run_b + M, A);
         }
         // the running sum after every pair is kept (transposed: element i of
-        // thread g at i*G + g) when every run of the group fits the buffer
+        // thread g at i*RS + g) when every run of the group fits the buffer
         const bool stored = sm.rates != nullptr &&
-                            (aligned ? static_cast<int>(grp.max_u32(static_cast<uint32_t>(run_e - run_b))) * G
-                                     : M * G) <= sm.rate_words;
+                            (aligned ? static_cast<int>(grp.max_u32(static_cast<uint32_t>(run_e - run_b))) * RS
+                                     : M * RS) <= sm.rate_words;
         float lsum = 0.0f;
         float *rp = stored ? sm.rates + g : nullptr;
         if (aligned) {
@@ -892,11 +909,11 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     lsum += ra;
                     if (rp) rp[0] = lsum;
                     lsum += rb;
-                    if (rp) { rp[G] = lsum; rp += 2 * G; }
+                    if (rp) { rp[RS] = lsum; rp += 2 * RS; }
                 }
                 if (col < Tc) {
                     lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    if (rp) { rp[0] = lsum; rp += G; }
+                    if (rp) { rp[0] = lsum; rp += RS; }
                 }
             }
         } else if (run_b < run_e) {
@@ -926,7 +943,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 lsum += ra;
                 if (rp) { rp[0] = lsum; }
                 lsum += rb;
-                if (rp) { rp[G] = lsum; rp += 2 * G; }
+                if (rp) { rp[RS] = lsum; rp += 2 * RS; }
                 // advance past the second pair
                 const bool wb = (colb + 1 == Tcb);
                 col = wb ? 0 : colb + 1;
@@ -1014,8 +1031,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             int idx = -1;
             for (int i0 = 0; i0 < len && idx < 0; i0 += 2 * G) {
                 const int ia = i0 + g, ib = i0 + G + g;
-                const float va = ia < len ? sm.rates[ia * G + L] : -1.0f;
-                const float vb = ib < len ? sm.rates[ib * G + L] : -1.0f;
+                const float va = ia < len ? sm.rates[ia * RS + L] : -1.0f;
+                const float vb = ib < len ? sm.rates[ib * RS + L] : -1.0f;
                 const int ha = grp.first(va >= rem);
                 const int hb = grp.first(vb >= rem);
                 if (ha >= 0) idx = i0 + ha;
@@ -1028,7 +1045,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 // with a positive rate
                 int lp = -1;
                 for (int i = g; i < len; i += G)
-                    if (sm.rates[i * G + L] > (i > 0 ? sm.rates[(i - 1) * G + L] : 0.0f)) lp = i;
+                    if (sm.rates[i * RS + L] > (i > 0 ? sm.rates[(i - 1) * RS + L] : 0.0f)) lp = i;
                 const int ll = static_cast<int>(grp.max_u32(static_cast<uint32_t>(lp + 1))) - 1;
                 if (ll >= 0) chosen = kbL + ll;
             }
@@ -1071,9 +1088,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 const int len = ke64 - kb64;
                 int c64 = -1, lp = -1;
                 for (int i = 0; i < len; ++i) {
-                    const float ri = sm.rates[i * G + L64];
+                    const float ri = sm.rates[i * RS + L64];
                     if (c64 < 0 && ri >= (rem64 > 0.0f ? rem64 : 1.0e-38f)) c64 = i;
-                    if (ri > (i > 0 ? sm.rates[(i - 1) * G + L64] : 0.0f)) lp = i;
+                    if (ri > (i > 0 ? sm.rates[(i - 1) * RS + L64] : 0.0f)) lp = i;
                 }
                 if (c64 < 0) c64 = lp;
                 if (kb64 + c64 != chosen) B.select_mismatch[c] += 1ull;
@@ -1431,7 +1448,7 @@ int launch_warp(const kmc_batch &b, cudaStream_t st)
     const int lw = chain_list_words<typename Pairs::Rec>(b.max_sites);
     int rw = rate_buffer_words(b.max_sites, G);
     // Pad each chain's area to G words modulo 32: the 32/G chains of a warp
-    // then store their running sums (element i of thread g at i*G + g) to
+    // then store their running sums (row i of the transposed layout) to
     // disjoint banks.
     if (G < 32) rw += ((G - (lw + rw)) % 32 + 32) % 32;
     if (static_cast<size_t>(wpb) * CPW * (lw + rw) * 4 > kSmemBudget) rw = 0;   // recompute instead
