@@ -114,6 +114,12 @@ inline int section_clocks_read(uint64_t *out, int reset)
 // 1-2.5 % slower than two-pair steps.
 constexpr int kPairUnroll = KMC_PAIR_UNROLL;
 
+// a compile-time bool as a type (selects a lambda's instantiation)
+template <bool V>
+struct BoolC {
+    static constexpr bool value = V;
+};
+
 __device__ __forceinline__ float ex2_approx(float x)
 {
     float y;
@@ -330,6 +336,9 @@ struct TablePairs {
         const float lcb = kUniform ? lb.y : fmaf(cs, lb.y, lb.x);
         return ex2_approx(fminf(lb.x, lcb - d));
     }
+    // the table carries the Coulomb term: no per-pair coefficient
+    __device__ __forceinline__ float rate_k(Rec s, Rec t, float /*k*/, float cs) const { return rate(s, t, false, cs); }
+    __device__ __forceinline__ static float coulomb_coef(float) { return 0.0f; }
     // Coulomb term I_0 R / d_jk between acceptors j, k (0 on the diagonal).
     __device__ __forceinline__ float coulomb(int j, int k) const
     {
@@ -369,6 +378,19 @@ struct PositionPairs {
         x = fmaxf(x, 0.0f);
         return ex2_approx(L - x);
     }
+    // The same rate with the Coulomb coefficient given: k = coulomb_coef(cs)
+    // for a pair of acceptors, 0 otherwise (fma(0, rs, x) is x exactly, so
+    // both forms give the same bits).
+    __device__ __forceinline__ float rate_k(Rec s, Rec t, float k, float /*cs*/) const
+    {
+        const float dx = t.x - s.x, dy = t.y - s.y, dz = t.z - s.z;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float rs = rsqrt_approx(d2);
+        const float L = fmaf(kL, d2 * rs, L0);
+        const float x = fmaxf(fmaf(k, rs, t.w - s.w), 0.0f);
+        return ex2_approx(L - x);
+    }
+    __device__ __forceinline__ float coulomb_coef(float cs) const { return -cs * IR; }
     __device__ __forceinline__ float coulomb(int j, int k) const
     {
         if (j == k) return 0.0f;
@@ -895,28 +917,40 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                                      : M * RS) <= sm.rate_words;
         float lsum = 0.0f;
         float *rp = stored ? sm.rates + g : nullptr;
-        if (aligned) {
+        // The pair walks, compiled once storing the running sums and once not
+        // (no per-pair test of the choice).
+        auto walk_aligned = [&](auto store) {
+            constexpr bool kStore = decltype(store)::value;
+            const float kacc = pairs.coulomb_coef(cs);
             for (int row = r0; row < r1; ++row) {
                 KMC_DCHECK(row >= 0 && row < h + P);
                 const Rec sr = sm.src[row];
                 const bool sa = row < h;
                 const int Tc = sa ? T1 : T2;
-                int col = 0;
+                // columns [0, z) are acceptors (with the Coulomb term when the
+                // source is one too), [z, Tc) electrodes
+                for (int seg = 0; seg < 2; ++seg) {
+                    const int c1 = seg ? Tc : z;
+                    const float k = (seg == 0 && sa) ? kacc : 0.0f;
+                    int col = seg ? z : 0;
 #pragma unroll kPairUnroll
-                for (; col + 1 < Tc; col += 2) {
-                    const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    const float rb = pairs.rate(sr, sm.tgt[col + 1], sa && col + 1 < z, cs);
-                    lsum += ra;
-                    if (rp) rp[0] = lsum;
-                    lsum += rb;
-                    if (rp) { rp[RS] = lsum; rp += 2 * RS; }
-                }
-                if (col < Tc) {
-                    lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                    if (rp) { rp[0] = lsum; rp += RS; }
+                    for (; col + 1 < c1; col += 2) {
+                        const float ra = pairs.rate_k(sr, sm.tgt[col], k, cs);
+                        const float rb = pairs.rate_k(sr, sm.tgt[col + 1], k, cs);
+                        lsum += ra;
+                        if constexpr (kStore) rp[0] = lsum;
+                        lsum += rb;
+                        if constexpr (kStore) { rp[RS] = lsum; rp += 2 * RS; }
+                    }
+                    if (col < c1) {
+                        lsum += pairs.rate_k(sr, sm.tgt[col], k, cs);
+                        if constexpr (kStore) { rp[0] = lsum; rp += RS; }
+                    }
                 }
             }
-        } else if (run_b < run_e) {
+        };
+        auto walk_balanced = [&](auto store) {
+            constexpr bool kStore = decltype(store)::value;
             // The thread walks its run in row-major order, two pairs per step
             // (two independent load -> rate chains; a row change is a select
             // plus a predicated reload, not a branch).
@@ -941,9 +975,9 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
                 const float rb = pairs.rate(srb, sm.tgt[colb], sab && colb < z, cs);
                 lsum += ra;
-                if (rp) { rp[0] = lsum; }
+                if constexpr (kStore) rp[0] = lsum;
                 lsum += rb;
-                if (rp) { rp[RS] = lsum; rp += 2 * RS; }
+                if constexpr (kStore) { rp[RS] = lsum; rp += 2 * RS; }
                 // advance past the second pair
                 const bool wb = (colb + 1 == Tcb);
                 col = wb ? 0 : colb + 1;
@@ -955,8 +989,15 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             }
             if (k < ke) {
                 lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                if (rp) rp[0] = lsum;
+                if constexpr (kStore) rp[0] = lsum;
             }
+        };
+        if (aligned) {
+            if (rp) walk_aligned(BoolC<true>{});
+            else walk_aligned(BoolC<false>{});
+        } else if (run_b < run_e) {
+            if (rp) walk_balanced(BoolC<true>{});
+            else walk_balanced(BoolC<false>{});
         }
         // the run [b, e) of thread l of the group
         auto run_of = [&](int l, int &b, int &e) {
