@@ -18,10 +18,10 @@ int launch_block_table(const kmc_batch &b, cudaStream_t st)
 int launch_block_positions(const kmc_batch &b, cudaStream_t st)
 {
     switch (b.lanes_per_chain) {
-    case 64: return launch_block<64, PositionPairs>(b, st);
-    case 128: return launch_block<128, PositionPairs>(b, st);
-    case 256: return launch_block<256, PositionPairs>(b, st);
-    case 512: return launch_block<512, PositionPairs>(b, st);
+    case 64: return launch_block<64, PairedPositionPairs>(b, st);
+    case 128: return launch_block<128, PairedPositionPairs>(b, st);
+    case 256: return launch_block<256, PairedPositionPairs>(b, st);
+    case 512: return launch_block<512, PairedPositionPairs>(b, st);
     default: return fail(KMC_ERR_INVALID, "engine: %d lanes per chain is not a block group", b.lanes_per_chain);
     }
 }

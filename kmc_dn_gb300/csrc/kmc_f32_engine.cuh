@@ -315,6 +315,7 @@ struct TablePairs {
     using Rec = int2;
     static constexpr bool kSiteInRec = true;    // rec.x is the site id
     static constexpr bool kUniformTable = kUniform;
+    static constexpr bool kPairedTgt = false;
     __device__ __forceinline__ static int site(Rec r) { return r.x; }
     const float2 *tab;
     const float *coul;   // kUniform: B of each pair
@@ -351,6 +352,7 @@ struct PositionPairs {
     using Rec = float4;
     static constexpr bool kSiteInRec = false;   // site ids kept beside the records
     static constexpr bool kUniformTable = false;
+    static constexpr bool kPairedTgt = false;
     __device__ __forceinline__ static int site(Rec) { return -1; }
     const float4 *pos;
     float kL, L0, IR;
@@ -399,6 +401,61 @@ struct PositionPairs {
         return IR * rsqrt_approx(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
     }
 };
+
+// Positions mode for block groups.  The target list is stored in pairs,
+// component by component ({x0, x1, y0, y1, z0, z1, w0, w1} for targets 2m
+// and 2m + 1), so two targets of a row load as two 16-byte words whose
+// halves are packed FP32 pairs, and the row-aligned walk evaluates both
+// pairs with the packed FP32x2 add / mul / fma (one instruction for two
+// pairs).  Each lane performs the operations of rate_k in the same order
+// with the same rounding: the rates are bit-identical to the scalar walk's.
+struct PairedPositionPairs : PositionPairs {
+    static constexpr bool kPairedTgt = true;
+    // targets (xy, zw) = {x0, x1, y0, y1}, {z0, z1, w0, w1} from a source
+    // whose negated record is ns, with Coulomb coefficient k (rate_k)
+    __device__ __forceinline__ void rate2(const float4 &xy, const float4 &zw, const float4 &ns, float k,
+                                          float &ra, float &rb) const
+    {
+        const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), make_float2(ns.x, ns.x));
+        const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), make_float2(ns.y, ns.y));
+        const float2 dz = __fadd2_rn(make_float2(zw.x, zw.y), make_float2(ns.z, ns.z));
+        const float2 d2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+        const float2 rs = make_float2(rsqrt_approx(d2.x), rsqrt_approx(d2.y));
+        const float2 L = __ffma2_rn(make_float2(kL, kL), __fmul2_rn(d2, rs), make_float2(L0, L0));
+        const float2 x = __ffma2_rn(make_float2(k, k), rs, __fadd2_rn(make_float2(zw.z, zw.w), make_float2(ns.w, ns.w)));
+        // L - max(x, 0) as L + min(-x, -0): the same value (signed zeros
+        // included, both give L when x <= 0)
+        const float2 y = __fadd2_rn(L, make_float2(fminf(-x.x, -0.0f), fminf(-x.y, -0.0f)));
+        ra = ex2_approx(y.x);
+        rb = ex2_approx(y.y);
+    }
+};
+
+// Target records: a plain array, or (kPairedTgt) pairs stored component by
+// component; col is the target's position in the list.
+template <typename Pairs>
+__device__ __forceinline__ typename Pairs::Rec tgt_load(const typename Pairs::Rec *t, int col)
+{
+    if constexpr (Pairs::kPairedTgt) {
+        const float *f = reinterpret_cast<const float *>(t) + (col >> 1) * 8 + (col & 1);
+        return make_float4(f[0], f[2], f[4], f[6]);
+    } else {
+        return t[col];
+    }
+}
+template <typename Pairs>
+__device__ __forceinline__ void tgt_store(typename Pairs::Rec *t, int col, const typename Pairs::Rec &r)
+{
+    if constexpr (Pairs::kPairedTgt) {
+        float *f = reinterpret_cast<float *>(t) + (col >> 1) * 8 + (col & 1);
+        f[0] = r.x;
+        f[2] = r.y;
+        f[4] = r.z;
+        f[6] = r.w;
+    } else {
+        t[col] = r;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Thread groups: a G-lane slice of a warp, or a whole block
@@ -634,8 +691,8 @@ struct BlockGroup {
 
 template <typename Rec>
 struct ChainSmem {
-    Rec *src;        // [S+1] source records
-    Rec *tgt;        // [S+1] target records
+    Rec *src;        // [S+2] source records
+    Rec *tgt;        // [S+2] target records (paired layout: tgt_load / tgt_store)
     int *src_id;     // [S+1] site ids of the sources
     int *tgt_id;     // [S+1] site ids of the targets
     float *E;        // [S]   site energies (acceptors), high part
@@ -654,7 +711,7 @@ __host__ __device__ __forceinline__ int chain_list_words(int S)
 {
     const int W = (S + 31) / 32;
     const int rw = static_cast<int>(sizeof(Rec) / 4);
-    const int words = 2 * rw * (S + 1) + 2 * (S + 1) + 2 * S + W + kMaxElectrodes;
+    const int words = 2 * rw * (S + 2) + 2 * (S + 1) + 2 * S + W + kMaxElectrodes;
     return (words + 3) & ~3;
 }
 
@@ -686,8 +743,8 @@ __device__ __forceinline__ ChainSmem<Rec> carve(uint32_t *base, int S, int rate_
 {
     ChainSmem<Rec> c;
     c.src = reinterpret_cast<Rec *>(base);
-    c.tgt = c.src + (S + 1);
-    c.src_id = reinterpret_cast<int *>(c.tgt + (S + 1));
+    c.tgt = c.src + (S + 2);
+    c.src_id = reinterpret_cast<int *>(c.tgt + (S + 2));
     c.tgt_id = c.src_id + (S + 1);
     c.E = reinterpret_cast<float *>(c.tgt_id + (S + 1));
     c.Elo = c.E + S;
@@ -818,7 +875,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 sm.src[below] = r;
                 if (!Pairs::kSiteInRec) sm.src_id[below] = j;
             } else {
-                sm.tgt[j - below] = r;
+                tgt_store<Pairs>(sm.tgt, j - below, r);
                 if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
             }
         }
@@ -826,7 +883,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             const Rec r = pairs.rec(N + e, cs * Vel[e]);
             if (e == g) el_rec = r;   // kept for the list rebuilds of later hops
             sm.src[h + e] = r;
-            sm.tgt[z + e] = r;
+            tgt_store<Pairs>(sm.tgt, z + e, r);
             if (!Pairs::kSiteInRec) {
                 sm.src_id[h + e] = N + e;
                 sm.tgt_id[z + e] = N + e;
@@ -933,17 +990,40 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     const int c1 = seg ? Tc : z;
                     const float k = (seg == 0 && sa) ? kacc : 0.0f;
                     int col = seg ? z : 0;
+                    if constexpr (Pairs::kPairedTgt) {
+                        // an odd first column alone, then whole target pairs:
+                        // two 16-byte loads and packed arithmetic per two pairs
+                        if ((col & 1) && col < c1) {
+                            lsum += pairs.rate_k(sr, tgt_load<Pairs>(sm.tgt, col), k, cs);
+                            if constexpr (kStore) { rp[0] = lsum; rp += RS; }
+                            ++col;
+                        }
+                        const float4 ns = make_float4(-sr.x, -sr.y, -sr.z, -sr.w);
+                        const float *tf = reinterpret_cast<const float *>(sm.tgt);
 #pragma unroll kPairUnroll
-                    for (; col + 1 < c1; col += 2) {
-                        const float ra = pairs.rate_k(sr, sm.tgt[col], k, cs);
-                        const float rb = pairs.rate_k(sr, sm.tgt[col + 1], k, cs);
-                        lsum += ra;
-                        if constexpr (kStore) rp[0] = lsum;
-                        lsum += rb;
-                        if constexpr (kStore) { rp[RS] = lsum; rp += 2 * RS; }
+                        for (; col + 1 < c1; col += 2) {
+                            const float4 xy = *reinterpret_cast<const float4 *>(tf + col * 4);
+                            const float4 zw = *reinterpret_cast<const float4 *>(tf + col * 4 + 4);
+                            float ra, rb;
+                            pairs.rate2(xy, zw, ns, k, ra, rb);
+                            lsum += ra;
+                            if constexpr (kStore) rp[0] = lsum;
+                            lsum += rb;
+                            if constexpr (kStore) { rp[RS] = lsum; rp += 2 * RS; }
+                        }
+                    } else {
+#pragma unroll kPairUnroll
+                        for (; col + 1 < c1; col += 2) {
+                            const float ra = pairs.rate_k(sr, tgt_load<Pairs>(sm.tgt, col), k, cs);
+                            const float rb = pairs.rate_k(sr, tgt_load<Pairs>(sm.tgt, col + 1), k, cs);
+                            lsum += ra;
+                            if constexpr (kStore) rp[0] = lsum;
+                            lsum += rb;
+                            if constexpr (kStore) { rp[RS] = lsum; rp += 2 * RS; }
+                        }
                     }
                     if (col < c1) {
-                        lsum += pairs.rate_k(sr, sm.tgt[col], k, cs);
+                        lsum += pairs.rate_k(sr, tgt_load<Pairs>(sm.tgt, col), k, cs);
                         if constexpr (kStore) { rp[0] = lsum; rp += RS; }
                     }
                 }
@@ -972,8 +1052,8 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 if (wa) srb = sm.src[rowb];        // reload only on a row change
                 const bool sab = rowb < h;
                 const int Tcb = sab ? T1 : T2;
-                const float ra = pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
-                const float rb = pairs.rate(srb, sm.tgt[colb], sab && colb < z, cs);
+                const float ra = pairs.rate(sr, tgt_load<Pairs>(sm.tgt, col), sa && col < z, cs);
+                const float rb = pairs.rate(srb, tgt_load<Pairs>(sm.tgt, colb), sab && colb < z, cs);
                 lsum += ra;
                 if constexpr (kStore) rp[0] = lsum;
                 lsum += rb;
@@ -988,7 +1068,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 Tc = sa ? T1 : T2;
             }
             if (k < ke) {
-                lsum += pairs.rate(sr, sm.tgt[col], sa && col < z, cs);
+                lsum += pairs.rate(sr, tgt_load<Pairs>(sm.tgt, col), sa && col < z, cs);
                 if constexpr (kStore) rp[0] = lsum;
             }
         };
@@ -1099,7 +1179,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 if (i < len) {
                     int row, col;
                     decode_pair(kb + i, h, A1, T1, T2, inv1, inv2, row, col);
-                    r = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
+                    r = pairs.rate(sm.src[row], tgt_load<Pairs>(sm.tgt, col), row < h && col < z, cs);
                 }
                 float ctot;
                 const float q = grp.scanf(r, ctot);
@@ -1146,7 +1226,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
         if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
 #endif
         const int from = Pairs::kSiteInRec ? Pairs::site(sm.src[row]) : sm.src_id[row];
-        const int to = Pairs::kSiteInRec ? Pairs::site(sm.tgt[col]) : sm.tgt_id[col];
+        const int to = Pairs::kSiteInRec ? Pairs::site(tgt_load<Pairs>(sm.tgt, col)) : sm.tgt_id[col];
         KMC_DCHECK(from >= 0 && from < S && to >= 0 && to < S && from != to && (from < N || to < N));
 #ifdef KMC_DEBUG_CHECKS
         if (grp.first(dbg_bad != 0) >= 0) { status = KMC_ERR_INVALID; break; }
@@ -1157,7 +1237,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
             B.hop_log[2 * li + 1] = to;
             if (B.hop_rates) {
                 B.hop_rates[2 * li] = totf;
-                B.hop_rates[2 * li + 1] = pairs.rate(sm.src[row], sm.tgt[col], row < h && col < z, cs);
+                B.hop_rates[2 * li + 1] = pairs.rate(sm.src[row], tgt_load<Pairs>(sm.tgt, col), row < h && col < z, cs);
             }
         }
         KMC_SECTION(4);
@@ -1176,7 +1256,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                 const Rec er = sm.src[h + e];
                 float part = 0.0f;
                 for (int k = g; k < N; k += G)
-                    part += (k < h) ? pairs.rate(sm.src[k], er, false, cs) : -pairs.rate(er, sm.tgt[k - h], false, cs);
+                    part += (k < h) ? pairs.rate(sm.src[k], er, false, cs) : -pairs.rate(er, tgt_load<Pairs>(sm.tgt, k - h), false, cs);
                 const float J = grp.sumf(part);
                 if (g == 0) B.flux_time[eoff + e] += static_cast<double>(J) * static_cast<double>(dt);
             }
@@ -1214,7 +1294,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     sm.src[below] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[below] = j;
                 } else {
-                    sm.tgt[j - below] = r;
+                    tgt_store<Pairs>(sm.tgt, j - below, r);
                     if (!Pairs::kSiteInRec) sm.tgt_id[j - below] = j;
                 }
             }
@@ -1223,7 +1303,7 @@ __device__ void run_chain(const kmc_batch &B, const Grp &grp, ChainSmem<typename
                     const Rec r = (e == g) ? el_rec : pairs.rec(N + e, cs * Vel[e]);
                     sm.src[h_new + e] = r;
                     if (!Pairs::kSiteInRec) sm.src_id[h_new + e] = N + e;
-                    sm.tgt[z_new + e] = r;
+                    tgt_store<Pairs>(sm.tgt, z_new + e, r);
                     if (!Pairs::kSiteInRec) sm.tgt_id[z_new + e] = N + e;
                 }
             }
