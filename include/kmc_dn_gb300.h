@@ -371,6 +371,15 @@ int kmc_section_clocks(uint64_t *cycles, int32_t reset);
  * reference counterpart (measurement support). */
 int kmc_measure_ex2_rate(double *ex2_per_second);
 
+/* Load every kernel of the library on the current device now.  CUDA loads
+ * a kernel's code lazily at its first launch, and that load waits for the
+ * kernels already running: a size class launched for the first time beside
+ * running ones (the uneven batch's bins on their own streams, a serving
+ * loop's new class) would otherwise start only when they end.  Idempotent;
+ * call once per device before concurrent launches.  No reference
+ * counterpart (the Go library runs on the host). */
+int kmc_preload_kernels(void);
+
 /*
  * Host-buffer batch run: chains on shared geometries, FP64 host inputs,
  * copies in and out inside the call (synchronous).  This is the

@@ -114,6 +114,7 @@ _SIGS = {
     "kmc_run_batch": (C.c_int, [C.POINTER(KmcBatch), _vp]),
     "kmc_engine_lane_options": (C.c_int, []),
     "kmc_measure_ex2_rate": (C.c_int, [C.POINTER(_f64)]),
+    "kmc_preload_kernels": (C.c_int, []),
     "kmc_section_clocks": (C.c_int, [_vp, _i32]),
     "kmc_run_batch_host": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
                                      _vp, _vp, _vp, _vp, _u64, _i32, _vp, _vp, _vp]),

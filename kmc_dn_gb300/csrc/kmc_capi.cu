@@ -103,6 +103,22 @@ static std::vector<int> chain_lanes(const HostRun &h)
     return g;
 }
 
+// Every kernel loaded once per device before a host path's first launches
+// (its size bins run side by side on their own streams).
+static int ensure_preloaded()
+{
+    int dev = 0;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGetDevice");
+    static std::mutex mu;
+    static uint64_t done = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 64 && ((done >> dev) & 1u)) return KMC_OK;
+    const int rc = kmc_preload_kernels();
+    if (rc == KMC_OK && dev < 64) done |= 1ull << dev;
+    return rc;
+}
+
 int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
 {
     *out = nullptr;
@@ -168,6 +184,7 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
     for (int G : lane_set)
         if (G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128 && G != 256 && G != 512)
             return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d", G);
+    if (int rc = ensure_preloaded(); rc != KMC_OK) return rc;
     const auto site_count = [&](int c) { return geom_N[chain_geom[c]] + geom_P[chain_geom[c]]; };
     // per bin (ascending lanes): its chains by size then hops, descending
     std::vector<std::vector<int32_t>> bin_work(lane_set.size());
@@ -656,6 +673,19 @@ int kmc_engine_read(kmc_engine *engine, double *time_out, int64_t *electrode_occ
 void kmc_engine_destroy(kmc_engine *engine)
 {
     delete reinterpret_cast<EngineState *>(engine);
+}
+
+int kmc_preload_kernels(void)
+{
+    int rc;
+    if ((rc = kmc::preload_warp_table()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_warp_positions()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_block()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_f64()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_setup()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_meanfield()) != KMC_OK) return rc;
+    if ((rc = kmc::preload_laplace()) != KMC_OK) return rc;
+    return kmc::ok();
 }
 
 }  // extern "C"

@@ -26,6 +26,24 @@ int launch_block_positions(const kmc_batch &b, cudaStream_t st)
     }
 }
 
+template <int T>
+static int preload_size()
+{
+    int rc;
+    if ((rc = preload_block_kernel<T, TablePairs<false>>()) != KMC_OK) return rc;
+    if ((rc = preload_block_kernel<T, TablePairs<true>>()) != KMC_OK) return rc;
+    return preload_block_kernel<T, PairedPositionPairs>();
+}
+
+int preload_block()
+{
+    int rc;
+    if ((rc = preload_size<64>()) != KMC_OK) return rc;
+    if ((rc = preload_size<128>()) != KMC_OK) return rc;
+    if ((rc = preload_size<256>()) != KMC_OK) return rc;
+    return preload_size<512>();
+}
+
 int section_clocks_block(uint64_t *out, int reset)
 {
 #ifdef KMC_SECTION_CLOCKS

@@ -1562,6 +1562,13 @@ int launch_warp_kernel(const kmc_batch &b, cudaStream_t st, int grid, size_t sme
 }
 
 template <int G, typename Pairs>
+int preload_warp_kernels()
+{
+    int rc;
+    if ((rc = touch_kernel(warp_engine_kernel<G, Pairs, 2>)) != KMC_OK) return rc;
+    return touch_kernel(warp_engine_kernel<G, Pairs, 3>);
+}
+template <int G, typename Pairs>
 int launch_warp(const kmc_batch &b, cudaStream_t st)
 {
     constexpr int CPW = 32 / G;
@@ -1612,6 +1619,11 @@ int launch_block_kernel(const kmc_batch &b, cudaStream_t st, size_t smem, int rw
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "engine launch");
 }
 
+template <int T, typename Pairs>
+int preload_block_kernel()
+{
+    return touch_kernel(block_engine_kernel<T, Pairs>);
+}
 template <int T, typename Pairs>
 int launch_block(const kmc_batch &b, cudaStream_t st)
 {

@@ -15,6 +15,15 @@ int launch_warp_positions(const kmc_batch &b, cudaStream_t st)
     }
 }
 
+int preload_warp_positions()
+{
+    int rc;
+    if ((rc = preload_warp_kernels<4, PositionPairs>()) != KMC_OK) return rc;
+    if ((rc = preload_warp_kernels<8, PositionPairs>()) != KMC_OK) return rc;
+    if ((rc = preload_warp_kernels<16, PositionPairs>()) != KMC_OK) return rc;
+    return preload_warp_kernels<32, PositionPairs>();
+}
+
 int section_clocks_warp_positions(uint64_t *out, int reset)
 {
 #ifdef KMC_SECTION_CLOCKS

@@ -15,6 +15,24 @@ int launch_warp_table(const kmc_batch &b, cudaStream_t st)
     }
 }
 
+template <int G>
+static int preload_width()
+{
+    int rc;
+    if ((rc = preload_warp_kernels<G, TablePairs<false>>()) != KMC_OK) return rc;
+    if ((rc = preload_warp_kernels<G, TablePairs<true>>()) != KMC_OK) return rc;
+    return preload_warp_kernels<G, TablePairs<true, true>>();
+}
+
+int preload_warp_table()
+{
+    int rc;
+    if ((rc = preload_width<4>()) != KMC_OK) return rc;
+    if ((rc = preload_width<8>()) != KMC_OK) return rc;
+    if ((rc = preload_width<16>()) != KMC_OK) return rc;
+    return preload_width<32>();
+}
+
 int section_clocks_warp_table(uint64_t *out, int reset)
 {
 #ifdef KMC_SECTION_CLOCKS

@@ -390,3 +390,14 @@ extern "C" int kmc_simulate_f64_static(int32_t n_acceptors, int32_t n_electrodes
                         ws, sizeof(double) * 3 * (size_t)kStaticWorkspaceSites * kStaticWorkspaceSites,
                         static_cast<cudaStream_t>(stream), nullptr);
 }
+
+namespace kmc {
+
+int preload_f64()
+{
+    int rc;
+    if ((rc = touch_kernel(f64_chain_kernel)) != KMC_OK) return rc;
+    return touch_kernel(f64_batch_kernel);
+}
+
+}  // namespace kmc

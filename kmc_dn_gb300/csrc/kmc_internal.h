@@ -27,6 +27,23 @@ int launch_block_positions(const kmc_batch &b, cudaStream_t st);
 int section_clocks_warp_table(uint64_t *out, int reset);
 int section_clocks_warp_positions(uint64_t *out, int reset);
 int section_clocks_block(uint64_t *out, int reset);
+// Load every kernel of a translation unit (kmc_preload_kernels).
+int preload_warp_table();
+int preload_warp_positions();
+int preload_block();
+int preload_f64();
+int preload_setup();
+int preload_meanfield();
+int preload_laplace();
+// Force the module loading of one kernel now (a kernel loaded lazily at its
+// first launch waits for the kernels already running on the device).
+template <typename K>
+inline int touch_kernel(K *kernel)
+{
+    cudaFuncAttributes a;
+    const cudaError_t e = cudaFuncGetAttributes(&a, reinterpret_cast<const void *>(kernel));
+    return e == cudaSuccess ? KMC_OK : fail_cuda(e, "kernel preload");
+}
 // Per-phase cycle counters of a -DKMC_SECTION_CLOCKS build (9 values).
 int section_clocks(uint64_t *out, int reset);
 int engine_smem_words(int max_sites);

@@ -202,3 +202,18 @@ extern "C" int kmc_p1_sample(int32_t nx, int32_t ny, double hx, double hy, int32
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "p1_sample launch");
 }
+
+namespace kmc {
+
+int preload_laplace()
+{
+    int rc;
+    if ((rc = touch_kernel(dst_basis_kernel)) != KMC_OK) return rc;
+    if ((rc = touch_kernel(rhs_kernel)) != KMC_OK) return rc;
+    if ((rc = touch_kernel(gemm_kernel)) != KMC_OK) return rc;
+    if ((rc = touch_kernel(scale_kernel)) != KMC_OK) return rc;
+    if ((rc = touch_kernel(scatter_kernel)) != KMC_OK) return rc;
+    return touch_kernel(p1_sample_kernel);
+}
+
+}  // namespace kmc

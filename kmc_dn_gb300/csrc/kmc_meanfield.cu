@@ -527,3 +527,14 @@ extern "C" int kmc_mf_run_host(const kmc_mf_batch *h, void *stream)
     cudaError_t e = cudaStreamSynchronize(st);
     return e == cudaSuccess ? KMC_OK : fail_cuda(e, "mf_run_host");
 }
+
+namespace kmc {
+
+int preload_meanfield()
+{
+    int rc;
+    if ((rc = touch_kernel(mf_kernel<true>)) != KMC_OK) return rc;
+    return touch_kernel(mf_kernel<false>);
+}
+
+}  // namespace kmc

@@ -140,3 +140,15 @@ extern "C" int kmc_measure_ex2_rate(double *ex2_per_second)
     *ex2_per_second = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
     return KMC_OK;
 }
+
+namespace kmc {
+
+int preload_setup()
+{
+    int rc;
+    if ((rc = touch_kernel(build_table_kernel)) != KMC_OK) return rc;
+    if ((rc = touch_kernel(site_energies_kernel)) != KMC_OK) return rc;
+    return touch_kernel(ex2_peak_kernel);
+}
+
+}  // namespace kmc

@@ -31,10 +31,22 @@ __all__ = ["simulate_f64", "TableSpec", "TableSet", "Batch", "simulate_cuda", "s
            "default_lanes", "make_work_lists", "device", "prune", "CancelWord", "simulate_f64_many"]
 
 
+_PRELOADED = set()
+
+
 def device(dev=None):
+    """The CUDA device to run on; on first use of a device every kernel of
+    the library is loaded there (kmc_preload_kernels), so that no launch
+    waits on a lazy code load behind the kernels already running."""
     if not torch.cuda.is_available():
         raise RuntimeError("kmc_dn_gb300 needs a CUDA device: the hop loop runs only as CUDA kernels")
-    return torch.device(dev if dev is not None else "cuda")
+    d = torch.device(dev if dev is not None else "cuda")
+    idx = d.index if d.index is not None else torch.cuda.current_device()
+    if idx not in _PRELOADED:
+        with torch.cuda.device(idx):
+            check(lib().kmc_preload_kernels())
+        _PRELOADED.add(idx)
+    return d
 
 
 def _ptr(t):
