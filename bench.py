@@ -414,9 +414,6 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--no-tail-lanes", action="store_true",
-                    help="uneven workload: keep every chain at its size class's lanes (no widening of the "
-                         "chains whose hop budgets would set the launch's length)")
     ap.add_argument("--persistent", action="store_true",
                     help="uneven workload: persistent launches (resident blocks claim work items)")
     ap.add_argument("--workload", default="homogeneous",
@@ -704,7 +701,7 @@ def bench_uneven(args):
               [net.electrodes[:, 3] for net, _ in nets], [net.occupation.astype(np.uint8) for net, _ in nets],
               hops, seed=args.seed + 5, pair_mode="positions", lanes=lanes,
               warps_per_block=(getattr(lanes, "warps", None) or 4) if lanes else 4,
-              persistent=args.persistent, tail_lanes=not args.no_tail_lanes)
+              persistent=args.persistent)
     streams = [torch.cuda.Stream() for _ in range(len(b._bins))]
     bin_ends = [torch.cuda.Event(enable_timing=True) for _ in b._bins]
     dt = _timed_launch(b, int(hops.max()), streams, bin_ends)
@@ -740,7 +737,6 @@ def bench_uneven(args):
                        "lanes": "autotuned per size class" if lanes else "default by size",
                        "launch": "persistent (work claimed with an atomic counter)" if args.persistent
                                  else "one work item per warp",
-                       "tail_lanes": not args.no_tail_lanes,
                        "autotune_s": tune_s,
                        "autotuned": {str(k): v for k, v in getattr(lanes, "picked", {}).items()}},
             "gpu_launches": len(b._bins), "n_pairs_per_s": float(r["n_pairs"].sum()) / dt}

@@ -315,52 +315,13 @@ _REANCHOR = 1024
 LANE_CHOICES = (4, 8, 16, 32, 64, 128, 256, 512)
 
 
-# Per-hop work of a group besides the pair walk (selection scan and search,
-# clock, list rebuild), in units of one thread's pair evaluations: warp
-# slices and block groups (whose steps end in block barriers); from the
-# section-clock split of a hop on GB300.
-_TAIL_FIXED = {True: 32.0, False: 96.0}
-# Threads that run pair walks side by side on a GB300 (152 SMs, register-
-# limited to about half of the 2048 threads an SM can hold).
-_TAIL_THREADS = 152 * 1024
-
-
-def widen_tail(S_c, hops, lane_of, slack=1.5, max_lanes=256, threads=_TAIL_THREADS):
-    """Wider groups for the chains that would set a launch's length.
-
-    With hop budgets that vary by orders of magnitude (log-uniform requests)
-    the launch lasts as long as its longest chain, which at the throughput-
-    optimal width is far longer than the batch's work spread over the GPU.
-    A chain's run takes about hops x (A/G + F) pair steps of one thread
-    (A ~ S^2/4 allowed pairs per hop, F the per-hop selection and update
-    work), the batch about sum(hops x A) / threads; a chain whose time exceeds
-    slack times that has its lanes doubled (into block groups past 32) while
-    that shortens it, up to max_lanes.  Returns the new lanes per chain."""
-    S = np.asarray(S_c, np.float64)
-    h = np.asarray(hops, np.float64)
-    A = np.maximum(S * S / 4.0, 1.0)
-    target = slack * float(np.sum(h * A)) / threads
-    out = np.asarray(lane_of, np.int32).copy()
-
-    def steps(G, a):
-        return a / G + _TAIL_FIXED[G <= 32]
-
-    for i in range(out.shape[0]):
-        G = int(out[i])
-        while G < max_lanes and h[i] * steps(G, A[i]) > target and steps(2 * G, A[i]) < steps(G, A[i]):
-            G *= 2
-        out[i] = G
-    return out
-
-
-def make_work_lists(S_c, hops, lanes=None, tail=False):
+def make_work_lists(S_c, hops, lanes=None):
     """Bin chains by lanes-per-chain and pack each bin into warp items.
 
     Returns a list of (G, work, order, max_sites): ``work`` holds 32/G chain
     ids per warp item (-1 pads the last item); chains are ordered by size,
     then hop budget (both descending) so that the chains sharing a warp have
-    similar per-hop work and similar lifetimes.  With ``tail``, the chains
-    that would set the launch's length get wider groups (``widen_tail``)."""
+    similar per-hop work and similar lifetimes."""
     S_c = np.asarray(S_c, np.int64).reshape(-1)
     hops = np.broadcast_to(np.asarray(hops, np.int64), S_c.shape)
     if lanes is None:
@@ -372,8 +333,6 @@ def make_work_lists(S_c, hops, lanes=None, tail=False):
     bad = set(lane_of.tolist()) - set(LANE_CHOICES)
     if bad:
         raise ValueError(f"lanes per chain must be one of {LANE_CHOICES}, got {sorted(bad)}")
-    if tail and S_c.shape[0] > 0:
-        lane_of = widen_tail(S_c, hops, lane_of)
     out = []
     for G in sorted(set(lane_of.tolist())):
         idx = np.flatnonzero(lane_of == G)
@@ -454,8 +413,6 @@ class Batch:
     record:      _native.RECORD_NONE / RECORD_NUMBA / RECORD_GO.
     lanes:       None (by size class), an int for every chain, or a callable
                  S -> lanes.
-    tail_lanes:  widen the groups of the chains whose hop budgets would
-                 otherwise set the launch's length (``widen_tail``).
     """
 
     def __init__(self, tables, chain_table, kT, E_constant=None,
@@ -463,7 +420,7 @@ class Batch:
                  record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
                  pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False,
-                 measure_drift=False, persistent=False, flux=False, tail_lanes=False):
+                 measure_drift=False, persistent=False, flux=False):
         self.dev = device(dev)
         d = self.dev
         tables_set = tables if isinstance(tables, TableSet) else None
@@ -563,7 +520,6 @@ class Batch:
         self.energy_drift = torch.zeros(n, dtype=torch.float32, device=d) if measure_drift else None
         self.cancel = None            # a CancelWord, or None
         self.time_budget_ns = 0       # per launch and chain; 0: none
-        self.tail_lanes = bool(tail_lanes)
         self._bins = self._make_bins(lanes, np.broadcast_to(np.asarray(hops, np.int64), (n,)))
         # persistent launches: one work counter per bin, zeroed before each launch
         self.persistent = bool(persistent)
@@ -581,7 +537,7 @@ class Batch:
     # -- work lists --------------------------------------------------------
     def _make_bins(self, lanes, hops):
         bins = []
-        for G, work, order, smax in make_work_lists(self.S_c, hops, lanes, tail=self.tail_lanes):
+        for G, work, order, smax in make_work_lists(self.S_c, hops, lanes):
             bins.append(dict(G=G, n_work=len(work) // max(1, 32 // G), work=_dev(work, torch.int32, self.dev),
                              max_sites=smax, chains=order))
         return bins

@@ -23,27 +23,6 @@ def test_work_lists_cover_every_chain_once():
     assert sorted(seen) == list(range(1000))
 
 
-def test_tail_widening_only_for_long_chains():
-    from kmc_dn_gb300.engine import widen_tail
-    rng = np.random.default_rng(1)
-    S = rng.integers(150, 212, 4000)
-    hops = np.full(4000, 10**4)
-    hops[:5] = 10**6                     # a few long requests in a batch of short ones
-    lanes = np.full(4000, 64)
-    w = widen_tail(S, hops, lanes)
-    assert np.all(w[:5] > 64) and np.all(w[:5] <= 256)
-    assert np.all(w[5:] == 64)
-    # equal budgets: nothing stands out, nothing changes
-    np.testing.assert_array_equal(widen_tail(S, np.full(4000, 10**5), lanes), lanes)
-    # the bins cover every chain once, the widened ones in the wider bins
-    seen = []
-    for G, work, order, smax in make_work_lists(S, hops, lanes=64, tail=True):
-        ids = work[work >= 0]
-        assert np.all(w[ids] == G)
-        seen.extend(ids.tolist())
-    assert sorted(seen) == list(range(4000))
-
-
 def test_work_lists_reject_bad_lanes():
     with pytest.raises(ValueError):
         make_work_lists([38], [10], lanes=6)
