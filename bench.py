@@ -865,17 +865,17 @@ def bench_meanfield(args):
             "gpu_launches": args.steps}
 
 
-def _serve_stream(srv, nets, rng, rate, window_s, drain_s, short_first=False):
+def _serve_stream(srv, nets, rng, rate, window_s, drain_s, short_first=False, budgets=(10_000, 100_000, 1_000_000)):
     """Submit a Poisson stream (``rate`` per second for ``window_s`` seconds)
     of voltage populations (32..512 vectors, U[-1,1]) on the resident
-    geometries with hop budgets from {1e4, 1e5, 1e6}, then wait up to
+    geometries with hop budgets from ``budgets``, then wait up to
     ``drain_s`` seconds for them.  With ``short_first`` only the 1e4-hop
     requests are waited for; the rest are cancelled after them.  Returns the
     requests (finished ones carry done_at)."""
     n_req = rng.poisson(rate * window_s)
     arr = np.cumsum(rng.exponential(1.0 / rate, n_req))
     spec = [(int(rng.integers(len(nets))), rng.uniform(-1, 1, (int(rng.integers(32, 513)), 8)),
-             int(rng.choice([10_000, 100_000, 1_000_000])), int(rng.integers(2**62))) for _ in range(n_req)]
+             int(rng.choice(list(budgets))), int(rng.integers(2**62))) for _ in range(n_req)]
     submitted = []
     t0 = time.perf_counter()
     for (g, V, h, sd), ta in zip(spec, arr):
@@ -900,7 +900,8 @@ def _serve_stream(srv, nets, rng, rate, window_s, drain_s, short_first=False):
     return submitted, time.perf_counter() - t0
 
 
-def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, sustainable_s=40.0):
+def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, sustainable_s=40.0,
+                   short_rate=8.0, short_s=12.0):
     """The serving loop on the voltage-search stream: 4 resident geometries
     (N in {30, 60, 120, 240}, M = 0.1 N, 8 electrodes), populations of
     32..512 voltage vectors, hop budgets {1e4, 1e5, 1e6}.
@@ -910,7 +911,11 @@ def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, susta
       can evaluate, so latency grows with the window): arrivals for
       ``window_s`` s, the 1e4-hop requests waited for, the rest cancelled;
     * at a sustainable rate (~70 % of capacity): arrivals for
-      ``sustainable_s`` s, all drained.
+      ``sustainable_s`` s, all drained;
+    * short requests only (1e4 hops, the voltage search's inner loop) at
+      ``short_rate`` per second for ``short_s`` s (about half of what the
+      device serves of them), all drained: enough of them per network size
+      for a p99 that is more than the largest of a handful.
     p50 / p99 latency (arrival to host result) per hop budget and, for the
     1e4-hop requests, per network size."""
     from kmc_dn_gb300 import workloads
@@ -949,9 +954,13 @@ def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, susta
     reqs, wall = _serve_stream(srv, nets, rng, sustainable_rate, sustainable_s, drain_s=120.0)
     sus = summary(reqs, wall)
     sus.update(rate_per_s=sustainable_rate, arrival_window_s=sustainable_s, hops_per_s=srv.hops_done / wall)
+    srv.hops_done = 0
+    reqs, wall = _serve_stream(srv, nets, rng, short_rate, short_s, drain_s=60.0, budgets=(10_000,))
+    short = summary(reqs, wall)
+    short.update(rate_per_s=short_rate, arrival_window_s=short_s, hops_per_s=srv.hops_done / wall)
     srv.stop(drain=False)
     return {"geometries_N": [n.N for n in nets], "isolated_1e4_hops_ms": isolated,
-            "at_specified_rate": over, "at_sustainable_rate": sus}
+            "at_specified_rate": over, "at_sustainable_rate": sus, "short_requests_at_sustainable_rate": short}
 
 
 def bench_serving(args):
