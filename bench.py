@@ -901,7 +901,7 @@ def _serve_stream(srv, nets, rng, rate, window_s, drain_s, short_first=False, bu
 
 
 def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, sustainable_s=40.0,
-                   short_rate=8.0, short_s=12.0):
+                   short_rate=8.0, short_s=12.0, **server_kw):
     """The serving loop on the voltage-search stream: 4 resident geometries
     (N in {30, 60, 120, 240}, M = 0.1 N, 8 electrodes), populations of
     32..512 voltage vectors, hop budgets {1e4, 1e5, 1e6}.
@@ -921,7 +921,7 @@ def serving_sample(seed=0, rate=200.0, window_s=0.5, sustainable_rate=1.0, susta
     from kmc_dn_gb300 import workloads
     from kmc_dn_gb300.serving import Server, latency_summary
     nets = workloads.serving_geometries(seed=seed)
-    srv = Server(nets, quantum=20480)
+    srv = Server(nets, quantum=20480, **server_kw)
     rng = np.random.Generator(np.random.PCG64(seed + 77))
     for g in range(len(nets)):          # warm-up: module load, allocator pools
         srv.submit(g, np.zeros((32, 8)), 2048, seed=g)

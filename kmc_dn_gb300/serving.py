@@ -53,6 +53,10 @@ from .engine import Batch, CancelWord, TableSet, TableSpec, _REANCHOR, superpose
 
 __all__ = ["Request", "Server", "latency_summary"]
 
+# Resident threads per SM of the engine's kernels at their register budgets
+# (block groups: 2 blocks of 256 threads at <= 128 registers).
+_ENGINE_THREADS_PER_SM = 512
+
 
 @dataclass(eq=False)          # identity: queue removal must not compare voltage arrays
 class Request:
@@ -89,6 +93,15 @@ class Server:
     quantum_long:   hops per launch of a long request (default 1024)
     short_lanes_factor: short requests run with this many times the default
                     threads per chain (lower latency, lower throughput)
+    short_thread_share: a short request's chains x threads per chain stay
+                    within this share of the engine's resident threads (512
+                    per SM at its register budgets), narrowing the groups of
+                    a large request, so that the next short request finds
+                    free SMs instead of waiting for a launch that fills them
+    short_big_quantum: hops per launch of a short request that holds at
+                    least half of that cap (a multiple of 1024; default
+                    2048): its blocks free up between quanta, where the next
+                    short request (less work, launched first) takes them
     short_hops:     requests with at most this many hops are short
     long_thread_share: fraction of the device's resident-thread slots that
                     long requests may hold (default 0.75)
@@ -104,14 +117,17 @@ class Server:
     def __init__(self, networks, *, quantum=4096, mem_budget=None,
                  pair_mode="positions", lanes=None, dev=None, short_hops=20000,
                  max_active_chains=16384, long_thread_share=0.75, quantum_long=_REANCHOR,
-                 short_lanes_factor=4, max_long_pause=1.0):
-        if quantum % _REANCHOR or quantum_long % _REANCHOR or quantum_long <= 0:
-            raise ValueError("quantum and quantum_long must be multiples of the re-anchor period (1024)")
+                 short_lanes_factor=4, max_long_pause=1.0, short_thread_share=0.5,
+                 short_big_quantum=2048):
+        if quantum % _REANCHOR or quantum_long % _REANCHOR or quantum_long <= 0 or \
+                short_big_quantum % _REANCHOR or short_big_quantum <= 0:
+            raise ValueError("quanta must be positive multiples of the re-anchor period (1024)")
         d = torch.device(dev if dev is not None else "cuda")
         self.dev = torch.device("cuda", d.index if d.index is not None else torch.cuda.current_device())
         self.networks = list(networks)
         self.quantum = int(quantum)
         self.quantum_long = int(quantum_long)
+        self.short_big_quantum = int(short_big_quantum)
         self.pair_mode = pair_mode
         self.lanes = lanes
         self.short_lanes_factor = int(short_lanes_factor)
@@ -124,6 +140,7 @@ class Server:
         props = torch.cuda.get_device_properties(self.dev)
         self.long_thread_budget = int(long_thread_share * props.multi_processor_count
                                       * props.max_threads_per_multi_processor)
+        self.short_thread_cap = int(short_thread_share * props.multi_processor_count * _ENGINE_THREADS_PER_SM)
         self.active_chains = 0
         self.active_long_chains = 0
         self.active_long_threads = 0
@@ -239,14 +256,30 @@ class Server:
     def _lanes(self, req):
         """Threads per chain: the throughput default, or for a short request
         a wider group (its latency is hops x per-hop time, and a wider group
-        cuts the per-hop time)."""
+        cuts the per-hop time), narrowed while the request's chains would
+        hold more than short_thread_cap threads: a request that fills the
+        SMs holds every block slot until its launch ends, and a wider group
+        past that point only adds waves."""
         if self.lanes is not None:
             return self.lanes
         if req.hops > self.short_hops or self.short_lanes_factor <= 1:
             return None
         from .engine import default_lanes
         net = self.networks[req.geometry]
-        return min(512, default_lanes(net.N + net.P) * self.short_lanes_factor)
+        G = min(512, default_lanes(net.N + net.P) * self.short_lanes_factor)
+        n = req.voltages.shape[0]
+        while G > 4 and n * G > self.short_thread_cap:
+            G //= 2
+        return G
+
+    def _quantum(self, req):
+        """Hops per launch: long requests short quanta; short ones one launch,
+        or short_big_quantum when they hold half the short-thread cap."""
+        if req.hops > self.short_hops:
+            return self.quantum_long
+        if 2 * self._threads(req) >= self.short_thread_cap:
+            return min(self.quantum, self.short_big_quantum)
+        return self.quantum
 
     def _threads(self, req):
         """Resident threads the request's chains occupy."""
@@ -335,7 +368,7 @@ class Server:
                 continue
             if not self._may_launch(req, short_busy, now):
                 continue
-            q = self.quantum if req.hops <= self.short_hops else self.quantum_long
+            q = self._quantum(req)
             seg = min(q, req.hops - req.launched_hops)
             seg_launch = ((seg + _REANCHOR - 1) // _REANCHOR) * _REANCHOR
             with torch.cuda.stream(req.stream):

@@ -139,6 +139,7 @@ def _admission_server(mem_budget, long_thread_budget):
     s.networks = [SimpleNamespace(N=30, P=8), SimpleNamespace(N=240, P=8)]
     s.queue, s.active, s.admitted = deque(), [], []
     s.lanes, s.short_lanes_factor, s.short_hops = None, 4, 20000
+    s.short_thread_cap = 152 * 512 // 2
     s.mem_budget, s.mem_used = mem_budget, 0
     s.max_active_chains, s.active_chains = 16384, 0
     s.long_thread_budget, s.active_long_threads = long_thread_budget, 0
@@ -186,6 +187,22 @@ def test_admission_caps_long_requests_but_not_short_ones():
     s.queue.append(short)
     s._admit()
     assert s.admitted == [long_a, short] and list(s.queue) == [long_b]
+
+
+def test_short_request_groups_narrow_to_leave_room():
+    """A short request widens its groups (lower latency) only while its
+    chains hold at most the short-thread cap; a large one narrows below the
+    default, so that the next short request finds free SMs."""
+    from kmc_dn_gb300.engine import default_lanes
+    from kmc_dn_gb300.serving import Request
+    s, _ = _admission_server(mem_budget=10**12, long_thread_budget=10**9)
+    cap = s.short_thread_cap
+    small = Request(0, np.zeros((32, 8)), 10**4, 1)          # N=30: 16 x 4 lanes
+    assert s._lanes(small) == 4 * default_lanes(38)
+    big = Request(1, np.zeros((512, 8)), 10**4, 2)           # N=240: 512 chains
+    G = s._lanes(big)
+    assert 512 * G <= cap and 512 * 2 * G > cap
+    assert s._lanes(Request(1, np.zeros((512, 8)), 10**6, 3)) is None   # long: the default
 
 
 def test_prune_cut_is_taken_in_float32_as_go_does():
