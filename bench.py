@@ -131,7 +131,7 @@ def cpu_baseline(net, V, threads, hops, n_chains, budget_s=20.0):
                       f"reference's Go simulate loop, no memo), {dt:.1f} s wall"}
 
 
-FLOOR = 0.05     # currents judged at the 1 % level: |I| >= 5 % of the voltage vector's largest |I|
+FLOOR = 0.05     # currents held to the 1 % level: |I| >= 5 % of the voltage vector's largest |I|
 
 
 def _current_stats(I32, I64):

@@ -59,7 +59,8 @@ def _stream_handle(stream=None):
 
 
 def _dev(a, dtype, dev):
-    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(dev)
+    # contiguous and writable (a broadcast view is read-only; torch warns on those)
+    return torch.as_tensor(np.require(a, requirements=("C", "W")), dtype=dtype).to(dev)
 
 
 # ---------------------------------------------------------------------------
