@@ -186,7 +186,10 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
             return fail(KMC_ERR_INVALID, "engine: lanes_per_chain %d", G);
     if (int rc = ensure_preloaded(); rc != KMC_OK) return rc;
     const auto site_count = [&](int c) { return geom_N[chain_geom[c]] + geom_P[chain_geom[c]]; };
-    // per bin (ascending lanes): its chains by size then hops, descending
+    // per bin (ascending lanes): its chains by size then hops, descending,
+    // where a warp item holds several chains; by work (hops x S^2, longest
+    // first) where an item is one chain, so the longest start in the first
+    // wave of blocks
     std::vector<std::vector<int32_t>> bin_work(lane_set.size());
     std::vector<int> bin_smax(lane_set.size(), 0);
     for (size_t k = 0; k < lane_set.size(); ++k) {
@@ -194,12 +197,16 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
         std::vector<int32_t> order;
         for (int c = 0; c < n_chains; ++c)
             if (lanes_of[c] == G) order.push_back(c);
+        const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
             const int sa = site_count(a), sb = site_count(b);
+            if (CPW == 1) {
+                const double wa = static_cast<double>(hops[a]) * sa * sa, wb = static_cast<double>(hops[b]) * sb * sb;
+                if (wa != wb) return wa > wb;
+            }
             if (sa != sb) return sa > sb;
             return hops[a] > hops[b];
         });
-        const int CPW = G >= 32 ? 1 : 32 / G;   // chains per warp, or one chain per block
         const size_t n_work = (order.size() + CPW - 1) / CPW;
         bin_work[k].assign(n_work * CPW, -1);
         for (size_t i = 0; i < order.size(); ++i) {

@@ -320,9 +320,13 @@ def make_work_lists(S_c, hops, lanes=None):
     """Bin chains by lanes-per-chain and pack each bin into warp items.
 
     Returns a list of (G, work, order, max_sites): ``work`` holds 32/G chain
-    ids per warp item (-1 pads the last item); chains are ordered by size,
-    then hop budget (both descending) so that the chains sharing a warp have
-    similar per-hop work and similar lifetimes."""
+    ids per warp item (-1 pads the last item).  Where a warp item holds
+    several chains they are ordered by size, then hop budget (both
+    descending), so that the chains sharing a warp have similar per-hop work
+    and similar lifetimes; where an item is one chain (G >= 32) they are
+    ordered by their work, hops x S^2, longest first, so that the longest
+    chains start in the first wave of blocks instead of setting the end of
+    the launch from a later one."""
     S_c = np.asarray(S_c, np.int64).reshape(-1)
     hops = np.broadcast_to(np.asarray(hops, np.int64), S_c.shape)
     if lanes is None:
@@ -337,8 +341,12 @@ def make_work_lists(S_c, hops, lanes=None):
     out = []
     for G in sorted(set(lane_of.tolist())):
         idx = np.flatnonzero(lane_of == G)
-        order = idx[np.lexsort((-hops[idx], -S_c[idx]))]
         cpw = max(1, 32 // G)
+        if cpw == 1:
+            work_est = hops[idx].astype(np.float64) * S_c[idx].astype(np.float64) ** 2
+            order = idx[np.lexsort((-hops[idx], -S_c[idx], -work_est))]
+        else:
+            order = idx[np.lexsort((-hops[idx], -S_c[idx]))]
         nw = (len(order) + cpw - 1) // cpw
         work = np.full(nw * cpw, -1, np.int32)
         work[: len(order)] = order

@@ -16,8 +16,12 @@ def test_work_lists_cover_every_chain_once():
         ids = work[work >= 0]
         assert np.all([default_lanes(int(S[i])) == G for i in ids])
         assert smax == S[ids].max()
-        # within a bin chains are sorted by size then hops (descending)
-        key = list(zip(-S[ids], -hops[ids]))
+        # within a bin: several chains per warp item sorted by size then hops,
+        # one chain per item by work hops x S^2 (all descending)
+        if G >= 32:
+            key = list(zip(-hops[ids] * S[ids].astype(float) ** 2, -S[ids], -hops[ids]))
+        else:
+            key = list(zip(-S[ids], -hops[ids]))
         assert key == sorted(key)
         seen.extend(ids.tolist())
     assert sorted(seen) == list(range(1000))
