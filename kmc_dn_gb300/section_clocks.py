@@ -7,7 +7,7 @@ engine compiled with -DKMC_SECTION_CLOCKS), runs one launch of the workload
 through it in a child process and prints one JSON line: for each phase of
 the hop loop, the cycles per hop seen by thread 0 of a group (its warp's
 time, including the issue slots other warps took) and its share.  The
-phases are those of csrc/kmc_f32.cu:
+phases are those of the hop loop in csrc/kmc_f32_engine.cuh:
 
   top       the cancel / time-budget / re-anchor checks at the top of a hop
   pairs     the rate walk over the thread's run of allowed pairs
