@@ -408,7 +408,10 @@ def main():
     ap.add_argument("--hops", type=int, default=HOPS)
     ap.add_argument("--chains", type=int, default=N_CHAINS)
     ap.add_argument("--lanes", type=int, default=0)
-    ap.add_argument("--warps-per-block", type=int, default=8)
+    # 7 warps: the ensemble's 2048 warp items make 293 blocks, at most two
+    # per SM (14 warps) on 152 SMs; 8 warps make 256 blocks, 104 SMs with
+    # two (16 warps) and 48 with one (+0.7 % measured for 7)
+    ap.add_argument("--warps-per-block", type=int, default=7)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")

@@ -103,6 +103,30 @@ static std::vector<int> chain_lanes(const HostRun &h)
     return g;
 }
 
+// Warps per block for a warp-slice bin of n_work warp items: the size that
+// puts the fewest warps on the busiest SM while every block is resident at
+// once at 16 warps per SM (2048 items on 152 SMs: 7 warps, 293 blocks, at
+// most 14 warps on an SM, where 8 warps leave 104 SMs with 16 and 48 with
+// 8); 8 when no size fits in one wave.
+static int balanced_warps_per_block(int n_work)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 8;
+    int best = 8, best_load = 0;
+    for (int w = 8; w >= 4; --w) {
+        const int blocks = (n_work + w - 1) / w;
+        if (blocks > (16 / w) * sms) continue;
+        const int load = ((blocks + sms - 1) / sms) * w;
+        if (best_load == 0 || load < best_load) {
+            best_load = load;
+            best = w;
+        }
+    }
+    return best;
+}
+
 // Every kernel loaded once per device before a host path's first launches
 // (its size bins run side by side on their own streams).
 static int ensure_preloaded()
@@ -398,6 +422,7 @@ int engine_run(EngineState &E, int64_t max_hops)
         b.max_sites = bn.max_sites;
         b.work = bn.work;
         b.n_work = bn.n_work;
+        if (bn.lanes <= 32) b.warps_per_block = balanced_warps_per_block(bn.n_work);
         const int rc = run_batch(b, k == 0 ? E.st : E.bin_streams[k - 1]);
         if (rc != KMC_OK) return rc;
     }
