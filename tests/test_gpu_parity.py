@@ -482,3 +482,20 @@ def test_uniform_temperature_table_guards_its_chains(engine_lib):
     b.uniform_kT = 0.75                     # as if the table were staged for another kT
     r = b.run().results()
     assert np.all(r["status"] == KMC_ERR_INVALID) and np.all(r["hops_done"] == 0)
+
+
+def test_preload_kernels_is_idempotent_and_launches_follow(engine_lib):
+    """kmc_preload_kernels loads every kernel of the library on the current
+    device (a lazily loaded kernel would wait for the size bins already
+    running); calling it again is a no-op, and launches work after it."""
+    from kmc_dn_gb300 import workloads
+    from kmc_dn_gb300.engine import Batch, TableSpec
+    assert engine_lib.kmc_preload_kernels() == 0
+    assert engine_lib.kmc_preload_kernels() == 0
+    net = workloads.plain_network(1)
+    spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
+    b = Batch([spec], np.zeros(4, np.int32), np.full(4, net.kT), np.tile(net.E_constant(), (4, 1)),
+              np.tile(net.electrodes[:, 3], (4, 1)), np.tile(net.occupation.astype(np.uint8), (4, 1)),
+              np.full(4, 2048), seed=3)
+    r = b.run().results()
+    assert np.all(r["status"] == 0) and np.all(r["hops_done"] == 2048)
