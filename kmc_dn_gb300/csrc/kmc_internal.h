@@ -46,7 +46,6 @@ inline int touch_kernel(K *kernel)
 }
 // Per-phase cycle counters of a -DKMC_SECTION_CLOCKS build (9 values).
 int section_clocks(uint64_t *out, int reset);
-int engine_smem_words(int max_sites);
 int build_table(int N, int P, double nu, double I0, double R, const double *d, const double *tc,
                 float *tab, cudaStream_t st);
 int site_energies(int n_chains, int N, int P, const double *basis, const double *V, double mu,
