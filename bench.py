@@ -408,10 +408,11 @@ def main():
     ap.add_argument("--hops", type=int, default=HOPS)
     ap.add_argument("--chains", type=int, default=N_CHAINS)
     ap.add_argument("--lanes", type=int, default=0)
-    # 7 warps: the ensemble's 2048 warp items make 293 blocks, at most two
-    # per SM (14 warps) on 152 SMs; 8 warps make 256 blocks, 104 SMs with
-    # two (16 warps) and 48 with one (+0.7 % measured for 7)
-    ap.add_argument("--warps-per-block", type=int, default=7)
+    # 0: the balanced size (engine.balanced_warps_per_block): 7 warps for the
+    # ensemble's 2048 warp items, 293 blocks, at most two per SM (14 warps)
+    # on 152 SMs, where 8 warps make 256 blocks, 104 SMs with two (16 warps)
+    # and 48 with one (+0.7 % measured for 7)
+    ap.add_argument("--warps-per-block", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
@@ -463,7 +464,7 @@ def main():
     lanes = args.lanes if args.lanes else None
     b = Batch([spec], np.zeros(n_chains, np.int32), np.full(n_chains, net.kT), None, None, occ0,
               np.full(n_chains, hops), streams=stream_ids, seed=args.seed + 1,
-              lanes=lanes, warps_per_block=args.warps_per_block, dev=dev, E_constant_dev=ec_dev,
+              lanes=lanes, warps_per_block=args.warps_per_block or None, dev=dev, E_constant_dev=ec_dev,
               el_energy_dev=vel_dev)
     occ_init = b.occupation.clone()
     stream = torch.cuda.Stream(device=dev)
@@ -570,7 +571,8 @@ def main():
                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": workload_config(n_chains, hops, world),
-               "engine": {"lanes_per_chain": b._bins[0]["G"], "warps_per_block": args.warps_per_block,
+               "engine": {"lanes_per_chain": b._bins[0]["G"],
+                          "warps_per_block": b._warps(b._bins[0]["G"], b._bins[0]["n_work"]),
                           "launches_per_step": launches_per_step, "graph_captured": True},
                "fp64_single_chain": {"value": f64_rate, "unit": "hops/s", "hops": f64_hops,
                                      "workload": "1 chain, same network, plain FP64 kernel"},

@@ -28,7 +28,8 @@ from . import _native
 from ._native import check, lib
 
 __all__ = ["simulate_f64", "TableSpec", "TableSet", "Batch", "simulate_cuda", "simulate_go", "superpose",
-           "default_lanes", "make_work_lists", "device", "prune", "CancelWord", "simulate_f64_many"]
+           "default_lanes", "make_work_lists", "device", "prune", "CancelWord", "simulate_f64_many",
+           "balanced_warps_per_block"]
 
 
 _PRELOADED = set()
@@ -316,6 +317,24 @@ _REANCHOR = 1024
 LANE_CHOICES = (4, 8, 16, 32, 64, 128, 256, 512)
 
 
+def balanced_warps_per_block(n_work, sms):
+    """Warps per block for a warp-slice launch of n_work warp items: the size
+    that puts the fewest warps on the busiest SM while every block is
+    resident at once at 16 warps per SM (2048 items on 152 SMs: 7 warps, 293
+    blocks, at most 14 warps on an SM, where 8 warps leave 104 SMs with 16
+    and 48 with 8); 8 when no size fits in one wave.  The C host path uses
+    the same rule."""
+    best, best_load = 8, None
+    for w in range(8, 3, -1):
+        blocks = (n_work + w - 1) // w
+        if blocks > (16 // w) * sms:
+            continue
+        load = ((blocks + sms - 1) // sms) * w
+        if best_load is None or load < best_load:
+            best, best_load = w, load
+    return best
+
+
 def make_work_lists(S_c, hops, lanes=None):
     """Bin chains by lanes-per-chain and pack each bin into warp items.
 
@@ -422,6 +441,10 @@ class Batch:
     record:      _native.RECORD_NONE / RECORD_NUMBA / RECORD_GO.
     lanes:       None (by size class), an int for every chain, or a callable
                  S -> lanes.
+    warps_per_block: warps per block of the warp-slice launches: an int, a
+                 dict or callable of the lanes per chain (as the autotuner
+                 returns them), or None for the balanced size of each bin
+                 (``balanced_warps_per_block``).
     """
 
     def __init__(self, tables, chain_table, kT, E_constant=None,
@@ -451,6 +474,7 @@ class Batch:
         # width (a dict G -> warps, or a callable G -> warps, as the
         # autotuner returns it)
         self.warps_per_block = warps_per_block
+        self._sms = torch.cuda.get_device_properties(d).multi_processor_count
 
         ts = tables_set if tables_set is not None else TableSet(self.tables, pair_mode=pair_mode, dev=d)
         self.table_set = ts
@@ -535,8 +559,10 @@ class Batch:
         self._counters = (torch.zeros(max(len(self._bins), 1), dtype=torch.int32, device=d)
                           if self.persistent else None)
 
-    def _warps(self, G):
+    def _warps(self, G, n_work=None):
         w = self.warps_per_block
+        if w is None:
+            return balanced_warps_per_block(n_work, self._sms) if n_work is not None and G <= 32 else 8
         if callable(w):
             w = w(G)
         elif isinstance(w, dict):
@@ -581,7 +607,7 @@ class Batch:
         b.n_work = bin_["n_work"]
         b.record = self.record
         b.reanchor = self.reanchor
-        b.warps_per_block = self._warps(bin_["G"])
+        b.warps_per_block = self._warps(bin_["G"], bin_["n_work"])
         b.max_hops_per_launch = int(seg)
         b.seed = self.seed
         if self.replay is not None:

@@ -47,7 +47,7 @@ def _measure(workload, hops):
         spec = TableSpec(net.N, net.P, net.nu, net.I_0, net.R, net.distances, net.transitions_constant)
         b = Batch([spec], np.zeros(n, np.int32), np.full(n, net.kT), [net.E_constant(v) for v in V], list(V),
                   np.tile(net.occupation.astype(np.uint8), (n, 1)), np.full(n, hops), seed=1, lanes=16,
-                  warps_per_block=8)
+                  warps_per_block=None)
         desc = "4096 chains, N=30 M=3 P=8, 16 lanes per chain, table mode"
     else:
         n = 256

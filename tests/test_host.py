@@ -27,6 +27,16 @@ def test_work_lists_cover_every_chain_once():
     assert sorted(seen) == list(range(1000))
 
 
+def test_balanced_warps_per_block():
+    """The launch shape that puts the fewest warps on the busiest SM, with
+    every block resident at once (16 warps per SM)."""
+    from kmc_dn_gb300.engine import balanced_warps_per_block as bw
+    assert bw(2048, 152) == 7          # 293 blocks: at most 14 warps on an SM (8 warps: 16)
+    assert bw(1024, 152) == 7          # 147 blocks, one per SM
+    assert bw(256, 152) == 4           # spread over more SMs
+    assert bw(5000, 152) == 8          # no size fits one wave
+
+
 def test_work_lists_reject_bad_lanes():
     with pytest.raises(ValueError):
         make_work_lists([38], [10], lanes=6)
