@@ -22,7 +22,6 @@ distributions of each workload:
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Optional
 
 import numpy as np
 
