@@ -25,7 +25,9 @@
 //               L and B come from a pair table (any tables the caller
 //               passes, shared by the chains of one geometry) or, in
 //               positions mode, from the sites' coordinates carried in the
-//               lists (d from one rsqrt; no table traffic).
+//               lists (d from one rsqrt; no table traffic; block groups
+//               keep the target list in component-wise pairs and evaluate
+//               two targets of a row with packed FP32x2 arithmetic).
 //  selection    The per-thread sums become 64-bit integers on a common
 //               power-of-two scale and are scanned exactly; the event is the
 //               first pair whose cumulative rate reaches u*total
