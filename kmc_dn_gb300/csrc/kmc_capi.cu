@@ -386,6 +386,10 @@ int engine_create(const HostRun &h, cudaStream_t user_stream, EngineState **out)
     b.occ_since = d_os;
     b.traffic = d_tr;
     b.reanchor = 1024;
+    // one temperature for every chain: the launch may stage (L, L + c B)
+    b.uniform_kT = 0.0f;
+    if (n_chains > 0 && std::all_of(kT32.begin(), kT32.end(), [&](float v) { return v == kT32[0]; }))
+        b.uniform_kT = kT32[0];
     b.warps_per_block = 8;
     b.max_hops_per_launch = 1024;
     b.seed = h.seed;
