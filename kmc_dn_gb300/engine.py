@@ -449,7 +449,7 @@ class Batch:
 
     def __init__(self, tables, chain_table, kT, E_constant=None,
                  el_energy=None, occupation=None, hops=None, *, streams=None, seed=0,
-                 record=_native.RECORD_NONE, lanes=None, warps_per_block=4, dev=None,
+                 record=_native.RECORD_NONE, lanes=None, warps_per_block=None, dev=None,
                  replay=None, E_constant_dev=None, el_energy_dev=None, reanchor=_REANCHOR,
                  pair_mode="table", hop_log=False, hop_rates=False, count_select_mismatch=False,
                  measure_drift=False, persistent=False, flux=False):
