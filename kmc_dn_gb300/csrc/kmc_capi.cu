@@ -93,12 +93,35 @@ struct EngineState {
 // Chains are binned by it and ordered inside a bin by size, then hop budget
 // (both descending), so that chains sharing a warp have similar per-hop work
 // and lifetimes -- the order of the Python Batch's work lists.
+// A launch of few chains cannot fill the GPU, and its run time is the
+// per-hop latency of one chain: each chain then gets a wider group (one
+// N=120 chain takes 2.7 us per hop at 256 lanes, 12.9 us at the size
+// default of 32), up to twice the next power of two of its site count and
+// 512 lanes, while the launch's chains x lanes stay within a quarter of the
+// engine's resident threads (512 per SM).  The Python layer applies the
+// same rule (engine.widen_small_launch).
+static int widen_small_launch(int G, int S, int n_chains, int sms)
+{
+    int p = 1;
+    while (p < S) p <<= 1;
+    const int target = std::min(512, 2 * p);
+    const int64_t budget = static_cast<int64_t>(sms) * 512 / 4;
+    while (G < target && static_cast<int64_t>(n_chains) * 2 * G <= budget) G *= 2;
+    return G;
+}
+
 static std::vector<int> chain_lanes(const HostRun &h)
 {
     std::vector<int> g(h.n_chains);
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 0;
     for (int c = 0; c < h.n_chains; ++c) {
         const int geo = h.chain_geom[c];
-        g[c] = h.lanes_per_chain > 0 ? h.lanes_per_chain : auto_lanes(h.geom_N[geo] + h.geom_P[geo]);
+        const int S = h.geom_N[geo] + h.geom_P[geo];
+        g[c] = h.lanes_per_chain > 0 ? h.lanes_per_chain
+                                     : widen_small_launch(auto_lanes(S), S, h.n_chains, sms);
     }
     return g;
 }

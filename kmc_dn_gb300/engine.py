@@ -29,7 +29,7 @@ from ._native import check, lib
 
 __all__ = ["simulate_f64", "TableSpec", "TableSet", "Batch", "simulate_cuda", "simulate_go", "superpose",
            "default_lanes", "make_work_lists", "device", "prune", "CancelWord", "simulate_f64_many",
-           "balanced_warps_per_block"]
+           "balanced_warps_per_block", "widen_small_launch"]
 
 
 _PRELOADED = set()
@@ -335,7 +335,24 @@ def balanced_warps_per_block(n_work, sms):
     return best
 
 
-def make_work_lists(S_c, hops, lanes=None):
+def widen_small_launch(G, S, n_chains, sms):
+    """Lanes for a chain of a launch too small to fill the GPU: its run time
+    is one chain's per-hop latency, so each chain gets a wider group (one
+    N=120 chain: 2.7 us per hop at 256 lanes, 12.9 us at the size default of
+    32), up to twice the next power of two of S and 512 lanes, while the
+    launch's chains x lanes stay within a quarter of the engine's resident
+    threads (512 per SM).  The C host path applies the same rule."""
+    p = 1
+    while p < S:
+        p <<= 1
+    target = min(512, 2 * p)
+    budget = sms * 512 // 4
+    while G < target and n_chains * 2 * G <= budget:
+        G *= 2
+    return G
+
+
+def make_work_lists(S_c, hops, lanes=None, sms=None):
     """Bin chains by lanes-per-chain and pack each bin into warp items.
 
     Returns a list of (G, work, order, max_sites): ``work`` holds 32/G chain
@@ -345,11 +362,15 @@ def make_work_lists(S_c, hops, lanes=None):
     and similar lifetimes; where an item is one chain (G >= 32) they are
     ordered by their work, hops x S^2, longest first, so that the longest
     chains start in the first wave of blocks instead of setting the end of
-    the launch from a later one."""
+    the launch from a later one.  With lanes None the size default applies,
+    widened for a launch too small to fill the GPU when the device's SM
+    count ``sms`` is given (``widen_small_launch``)."""
     S_c = np.asarray(S_c, np.int64).reshape(-1)
     hops = np.broadcast_to(np.asarray(hops, np.int64), S_c.shape)
     if lanes is None:
-        lane_of = np.array([default_lanes(int(s)) for s in S_c], np.int32)
+        n = S_c.shape[0]
+        lane_of = np.array([default_lanes(int(s)) if sms is None else
+                            widen_small_launch(default_lanes(int(s)), int(s), n, sms) for s in S_c], np.int32)
     elif callable(lanes):
         lane_of = np.array([int(lanes(int(s))) for s in S_c], np.int32)
     else:
@@ -572,7 +593,7 @@ class Batch:
     # -- work lists --------------------------------------------------------
     def _make_bins(self, lanes, hops):
         bins = []
-        for G, work, order, smax in make_work_lists(self.S_c, hops, lanes):
+        for G, work, order, smax in make_work_lists(self.S_c, hops, lanes, sms=self._sms):
             bins.append(dict(G=G, n_work=len(work) // max(1, 32 // G), work=_dev(work, torch.int32, self.dev),
                              max_sites=smax, chains=order))
         return bins

@@ -27,6 +27,20 @@ def test_work_lists_cover_every_chain_once():
     assert sorted(seen) == list(range(1000))
 
 
+def test_small_launches_get_wider_groups():
+    """A launch too small to fill the GPU widens each chain's group (lower
+    per-hop latency); a full one keeps the size default."""
+    from kmc_dn_gb300.engine import widen_small_launch as w
+    assert w(16, 38, 1, 152) == 128            # one N=30 chain: up to 2 x next_pow2(38)
+    assert w(32, 128, 1, 152) == 256           # one N=120 chain
+    assert w(256, 1008, 1, 152) == 512         # capped at 512 lanes
+    assert w(16, 38, 4096, 152) == 16          # the 4096-chain ensemble fills the GPU
+    assert w(16, 38, 200, 152) == 64           # 200 x 64 x 2 exceeds a quarter of 152 x 512
+    S = np.array([38] * 3 + [128] * 2)
+    for G, work, order, smax in make_work_lists(S, np.full(5, 1000), sms=152):
+        assert G == (128 if smax == 38 else 256)
+
+
 def test_balanced_warps_per_block():
     """The launch shape that puts the fewest warps on the busiest SM, with
     every block resident at once (16 warps per SM)."""
