@@ -41,6 +41,18 @@ def test_small_launches_get_wider_groups():
         assert G == (128 if smax == 38 else 256)
 
 
+def test_short_request_quanta():
+    """Long requests run in long-request quanta; a short request runs in one
+    launch unless it holds a quarter of the resident threads, when it runs in
+    short_big_quantum hops so that its blocks free up for the next one."""
+    from kmc_dn_gb300.serving import Request
+    s, _ = _admission_server(mem_budget=10**12, long_thread_budget=10**9)
+    s.quantum, s.quantum_long, s.short_big_quantum = 20480, 1024, 2048
+    assert s._quantum(Request(0, np.zeros((32, 8)), 10**4, 1)) == 20480     # 32 x 64 threads
+    assert s._quantum(Request(1, np.zeros((512, 8)), 10**4, 2)) == 2048     # 512 x 64 threads
+    assert s._quantum(Request(1, np.zeros((512, 8)), 10**6, 3)) == 1024     # long
+
+
 def test_balanced_warps_per_block():
     """The launch shape that puts the fewest warps on the busiest SM, with
     every block resident at once (16 warps per SM)."""
